@@ -1,0 +1,72 @@
+// capi_internal.h -- host-side state behind the C ABI handles.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/genie_gb300.h"
+#include "host_index.h"
+#include "match.cuh"
+
+namespace gg {
+
+int fail(int code, const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+
+// One growable device allocation.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t reserve(size_t want);
+    void release();
+};
+
+struct DeviceContext {
+    bool ready = false;
+    int num_sms = 0;
+    Tuning tuning;
+};
+DeviceContext &device_context(int dev);
+
+// Device buffers of one in-flight search (query inputs, plan, work lists,
+// part scratch, results), grown on demand.
+struct Workspace {
+    DevBuf item_off, dim, low, up, weight, weighted, k, out_off;
+    DevBuf span_start, span_len, inc, qinfo, work, ctr, qstate, done, part_cnt, scratch;
+    DevBuf out_ids, out_counts, out_scores;
+    bool done_zeroed = false;
+    int64_t done_q = 0;
+    cudaError_t reserve(int64_t Q, int64_t items, int64_t sumk);
+    void release();
+    Work view(int64_t Q, bool scores) const;
+};
+
+int validate_queries(const genie_queries *q, std::vector<int64_t> &out_off, int64_t &n_items);
+int check_device_error(uint32_t err);
+
+}  // namespace gg
+
+struct genie_index {
+    int device = 0;
+    bool is_bag = false;
+    gg::HostIndex host;              // host mirror: bounds and key offsets (ids live on the device)
+    int64_t n_ids = 0;
+    int32_t codec = 0;
+    int32_t max_seg = 0;
+    int64_t n_words = 0;
+    int64_t n_segs = 0;
+    gg::DevBuf d_ids, d_key_off, d_key_base, d_dim_min, d_dim_max;
+    gg::DevBuf d_words, d_key_seg, d_seg_word_off, d_seg_first, d_seg_len;
+    gg::DevIndex dev{};
+    gg::Tuning tuning{};
+    cudaStream_t stream = nullptr;
+    std::mutex mu;                   // serialises searches on this handle's workspace
+    gg::Workspace ws;
+    uint32_t *host_err = nullptr;    // pinned error word of the last search
+    int last_launches = 0;
+    ~genie_index();
+};

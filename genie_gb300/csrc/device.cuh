@@ -1,0 +1,241 @@
+// device.cuh -- shared device-side types and primitives of the match path.
+//
+// Layout in HBM (one resident index):
+//   ids       u32[n_ids (+pad)]   posting ids, ordered by (dim, value, id)
+//                                 -- identical to the reference's inv_table::_inv
+//                                 (table/inv_table.cu:281-337)
+//   key_off   i64[n_keys+1]       start of each (dim,value) list in ids
+//   key_base  i64[D+1]            first key of each dim (no 16-bit value limit,
+//                                 unlike the reference's (dim<<16)+value keys,
+//                                 table/inv_table.h:212)
+//   dim_min / dim_max i32[D]      value bounds of each dim
+// A compressed index adds the reference codec segments (see codecs.cuh).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gg {
+
+constexpr int kMaxParts = 16;        // id-range parts of one query
+constexpr int kMaxK = 2048;          // largest k per query
+constexpr int kItemChunk = 512;      // query items staged in shared memory at once
+constexpr int kCandCap = 2048;       // candidate buffer of the top-k selection
+
+enum : uint8_t { kClsNone = 0, kClsSparse = 1, kClsDense = 2 };
+enum : uint8_t { kFlagWeighted = 1, kFlagSmallCount = 2, kFlagRetry = 4, kFlagPacked = 8 };
+enum : uint32_t { kErrWeight = 1, kErrOverflow = 2, kErrCapacity = 4 };
+
+struct DevIndex {
+    const uint32_t *ids;
+    const int64_t *key_off;
+    const int64_t *key_base;
+    const int32_t *dim_min;
+    const int32_t *dim_max;
+    int64_t n_objects;
+    int64_t n_ids;
+    int32_t n_dims;
+    int32_t mult_max;
+    // compressed layout (codec != 0)
+    int32_t codec;
+    int32_t max_seg;
+    const uint32_t *words;
+    const int64_t *key_seg;
+    const int64_t *seg_word_off;
+    const uint32_t *seg_first;
+    const uint32_t *seg_len;
+};
+
+struct DevQueries {
+    int32_t n_queries;
+    const int64_t *item_off;
+    const int32_t *dim;
+    const int32_t *low;
+    const int32_t *up;
+    const float *weight;
+    const uint8_t *weighted;
+    const uint32_t *k;
+    uint32_t uniform_k;
+    const int64_t *out_off;
+};
+
+// Per-query plan written by k_plan.
+struct QInfo {
+    int64_t total;      // posting ids touched (sum of span lengths)
+    int64_t item0;      // first item
+    int32_t n_items;
+    uint32_t k;
+    int32_t scale;      // fixed-point exponent of a weighted query
+    uint16_t parts;     // id-range parts
+    uint8_t cls;        // kClsSparse / kClsDense / kClsNone
+    uint8_t flags;
+};
+
+struct Tuning {
+    int32_t sparse_slots_packed;   // hash slots per CTA, 4-byte entries
+    int32_t sparse_slots_wide;     // hash slots per CTA, 8-byte entries
+    int32_t sparse_threads;
+    int32_t dense_tile_u8;         // ids per tile, 1-byte counters
+    int32_t dense_tile_u32;        // ids per tile, 4-byte counters
+    int32_t dense_threads;
+    int64_t sparse_max_total;      // more touched ids than this -> dense
+    int64_t dense_part_work;       // touched ids per dense part
+    int32_t sparse_ctas_per_sm;
+    int32_t dense_ctas_per_sm;
+};
+
+// Work lists, one per kernel variant.
+enum : int { kListSparsePacked = 0, kListSparseWide = 1, kListDenseSmall = 2, kListDenseWide = 3,
+             kNumLists = 4 };
+constexpr int kCtrError = 2 * kNumLists;     // ctr[2c] = items in list c, ctr[2c+1] = next
+constexpr int kCtrWords = 2 * kNumLists + 2;
+
+// Device work state of one search (all arrays sized for the batch).
+struct Work {
+    int64_t *span_start;   // [items] global position of the item's span
+    int64_t *span_len;     // [items]
+    uint32_t *inc;         // [items] increment per match (1, or fixed-point weight)
+    QInfo *qinfo;          // [Q]
+    uint2 *work;           // [kNumLists][Q*kMaxParts] (query, part)
+    int64_t work_stride;   // Q*kMaxParts
+    uint32_t *ctr;         // [kCtrWords]
+    uint32_t *qstate;      // [Q] bit0: a sparse part overflowed
+    uint32_t *done;        // [Q] finished parts
+    uint32_t *part_cnt;    // [Q*kMaxParts]
+    uint64_t *scratch;     // [sum(k)*kMaxParts] part results (keys)
+    uint32_t *out_ids;
+    uint32_t *out_counts;
+    float *out_scores;     // may be null
+};
+
+// ---------------------------------------------------------------- helpers
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ uint32_t warp_id() { return threadIdx.x >> 5; }
+
+// First position p in [lo, hi) with ids[p] >= x.
+__device__ __forceinline__ int64_t lower_bound_u32(const uint32_t *__restrict__ a, int64_t lo,
+                                                   int64_t hi, uint32_t x) {
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (__ldg(a + mid) < x) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Galloping search from lo: first position in [lo, hi) with a[p] >= x.
+__device__ __forceinline__ int64_t gallop_u32(const uint32_t *__restrict__ a, int64_t lo,
+                                              int64_t hi, uint32_t x) {
+    if (lo >= hi || __ldg(a + lo) >= x) return lo;
+    int64_t step = 1, prev = lo;
+    while (true) {
+        int64_t probe = prev + step;
+        if (probe >= hi) return lower_bound_u32(a, prev + 1, hi, x);
+        if (__ldg(a + probe) >= x) return lower_bound_u32(a, prev + 1, probe, x);
+        prev = probe;
+        step <<= 1;
+    }
+}
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if ((int)lane_id() >= o) v += t;
+    }
+    return v;
+}
+
+__device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide exclusive scan of one u32 per thread; s_tmp holds >= 33 words.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *s_tmp, uint32_t *total) {
+    const uint32_t nw = (blockDim.x + 31) >> 5;
+    uint32_t incl = warp_incl_scan(v);
+    __syncthreads();
+    if (lane_id() == 31) s_tmp[warp_id()] = incl;
+    __syncthreads();
+    if (warp_id() == 0) {
+        uint32_t x = lane_id() < nw ? s_tmp[lane_id()] : 0u;
+        uint32_t xi = warp_incl_scan(x);
+        if (lane_id() < nw) s_tmp[lane_id()] = xi - x;
+        if (lane_id() == nw - 1) s_tmp[32] = xi;
+    }
+    __syncthreads();
+    uint32_t r = s_tmp[warp_id()] + incl - v;
+    if (total) *total = s_tmp[32];
+    __syncthreads();
+    return r;
+}
+
+// Warp-aggregated shared-memory histogram increment: lanes holding the same
+// bin combine into one atomic (__match_any_sync).  All 32 lanes must call.
+__device__ __forceinline__ void hist_add(uint32_t *hist, uint32_t bin, bool active) {
+    uint32_t act = __ballot_sync(0xffffffffu, active);
+    if (!active) return;
+    uint32_t peers = __match_any_sync(act, bin);
+    if (lane_id() == (uint32_t)(__ffs(peers) - 1)) atomicAdd(&hist[bin], (uint32_t)__popc(peers));
+}
+
+// Result key: primary (count or fixed-point weight sum) high, inverted id low,
+// so that a larger key ranks first and equal primaries rank by ascending id.
+__device__ __forceinline__ uint64_t make_key(uint32_t prim, uint32_t id) {
+    return ((uint64_t)prim << 32) | (uint64_t)(0xFFFFFFFFu - id);
+}
+__device__ __forceinline__ uint32_t key_prim(uint64_t k) { return (uint32_t)(k >> 32); }
+__device__ __forceinline__ uint32_t key_id(uint64_t k) { return 0xFFFFFFFFu - (uint32_t)k; }
+
+// Descending bitonic sort of n (power of two) keys in shared memory.
+__device__ __forceinline__ void bitonic_sort_desc(uint64_t *a, uint32_t n) {
+    for (uint32_t size = 2; size <= n; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            __syncthreads();
+            for (uint32_t t = threadIdx.x; t < n / 2; t += blockDim.x) {
+                uint32_t i = 2 * t - (t & (stride - 1));
+                uint32_t j = i + stride;
+                bool desc = ((i & size) == 0);
+                uint64_t x = a[i], y = a[j];
+                if ((x < y) == desc) { a[i] = y; a[j] = x; }
+            }
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ uint32_t next_pow2(uint32_t v) {
+    return v <= 1 ? 1u : 1u << (32 - __clz(v - 1));
+}
+
+// Write the final k results of query q from sorted keys.
+__device__ __forceinline__ void write_results(const Work &W, int64_t out_off, uint32_t k,
+                                              const uint64_t *sorted, uint32_t n, bool weighted,
+                                              int32_t scale) {
+    for (uint32_t j = threadIdx.x; j < k; j += blockDim.x) {
+        uint32_t id = 0, cnt = 0;
+        float sc = 0.0f;
+        if (j < n) {
+            uint64_t key = sorted[j];
+            uint32_t prim = key_prim(key);
+            id = key_id(key);
+            if (weighted) {
+                sc = __double2float_rn(ldexp((double)prim, -scale));
+                cnt = (uint32_t)sc;              // (int) aggregation, knn.cu:54
+            } else {
+                cnt = prim;
+                sc = (float)prim;
+            }
+        }
+        W.out_ids[out_off + j] = id;
+        W.out_counts[out_off + j] = cnt;
+        if (W.out_scores) W.out_scores[out_off + j] = sc;
+    }
+}
+
+}  // namespace gg
+
+namespace gg {
+__device__ __forceinline__ uint64_t umin64(uint64_t a, uint64_t b) { return a < b ? a : b; }
+}  // namespace gg

@@ -1,0 +1,653 @@
+// match.cu -- the match-count hot path: query plan, sparse (hash) and dense
+// (id-tiled) counting kernels, exact top-k and the cross-part merge.
+//
+// Reference counterpart: matching::match / match_AT (matching/match.cu:43-464),
+// the c-PQ and bitmap counters (matching/match_device_utils.h:160-473),
+// convert_to_data + heap_count_topk (match_common.cu:9-20, heap_count.cu:24-282)
+// and extract_index_and_count (knn.cu:47-55).  The reference counts every
+// posting id with a global-memory atomicCAS on a packed per-query bitmap and
+// probes a per-query global hash; here every count lives in shared memory.
+#include "match.cuh"
+#include "select.cuh"
+
+#include <algorithm>
+#include <cstdio>
+
+namespace gg {
+
+// ------------------------------------------------------------------ plan
+
+// One warp per query: items -> spans (Query::build, query/query.cc:273-333),
+// per-item increments, the fixed-point scale of weighted queries, and the
+// sparse/dense decision with the number of id-range parts.
+__global__ void __launch_bounds__(256) k_plan(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (q >= Q.n_queries) return;
+    const uint32_t lane = lane_id();
+    const int64_t i0 = Q.item_off[q], i1 = Q.item_off[q + 1];
+    const int32_t m = (int32_t)(i1 - i0);
+    const uint32_t k = Q.k ? Q.k[q] : Q.uniform_k;
+    const bool weighted = Q.weighted && Q.weight && Q.weighted[q];
+    int32_t scale = 0;
+    if (weighted) {
+        int bad = 0;
+        if (lane == 0) {
+            double s = 0.0;
+            for (int64_t i = i0; i < i1; ++i) {
+                float w = Q.weight[i];
+                if (!(w > 0.0f) || isinf(w)) bad = 1;
+                s += (double)w;
+            }
+            int e = 0;
+            (void)frexp(s, &e);
+            scale = 31 - e;
+        }
+        scale = __shfl_sync(0xffffffffu, scale, 0);
+        bad = __shfl_sync(0xffffffffu, bad, 0);
+        if (bad && lane == 0) atomicOr(&W.ctr[kCtrError], kErrWeight);
+    }
+    int64_t total = 0;
+    for (int64_t i = i0 + lane; i < i1; i += 32) {
+        int32_t d = Q.dim[i], lo = Q.low[i], hi = Q.up[i];
+        int64_t start = 0, end = 0;
+        if (d >= 0 && d < ix.n_dims) {
+            int32_t mn = ix.dim_min[d], mx = ix.dim_max[d];
+            if (!(lo > hi || lo > mx || hi < mn)) {
+                if (lo < mn) lo = mn;
+                if (hi > mx) hi = mx;
+                int64_t k0 = ix.key_base[d] + ((int64_t)lo - mn);
+                int64_t k1 = ix.key_base[d] + ((int64_t)hi - mn) + 1;
+                start = ix.key_off[k0];
+                end = ix.key_off[k1];
+            }
+        }
+        W.span_start[i] = start;
+        W.span_len[i] = end - start;
+        uint32_t inc = 1;
+        if (weighted) inc = (uint32_t)__double2ll_rn(ldexp((double)Q.weight[i], scale));
+        W.inc[i] = inc;
+        total += end - start;
+    }
+    total = (int64_t)warp_sum_u64((uint64_t)total);
+    if (lane == 0) {
+        QInfo qi;
+        qi.total = total;
+        qi.item0 = i0;
+        qi.n_items = m;
+        qi.k = k;
+        qi.scale = scale;
+        qi.flags = weighted ? kFlagWeighted : 0;
+        const bool small = !weighted && (int64_t)m * ix.mult_max <= 255;
+        if (small) qi.flags |= kFlagSmallCount;
+        qi.parts = 1;
+        qi.cls = kClsNone;
+        int list = -1;
+        if (k == 0 || k > (uint32_t)kMaxK) atomicOr(&W.ctr[kCtrError], kErrCapacity);
+        else if (total > 0) {
+            const bool packed = small && ix.n_objects <= (int64_t)(1u << 24);
+            const int64_t slots = packed ? T.sparse_slots_packed : T.sparse_slots_wide;
+            const int64_t cap = slots * 3 / 4;
+            const int64_t ps = (total + cap - 1) / cap;
+            if (total <= T.sparse_max_total && ps <= kMaxParts && total * 4 <= ix.n_objects * 3) {
+                qi.cls = kClsSparse;
+                qi.parts = (uint16_t)ps;
+                if (packed) qi.flags |= kFlagPacked;
+                list = packed ? kListSparsePacked : kListSparseWide;
+            } else {
+                qi.cls = kClsDense;
+                const int64_t tile = small ? T.dense_tile_u8 : T.dense_tile_u32;
+                const int64_t ntiles = (ix.n_objects + tile - 1) / tile;
+                int64_t pd = (total + T.dense_part_work - 1) / T.dense_part_work;
+                pd = pd < 1 ? 1 : pd;
+                pd = pd > ntiles ? ntiles : pd;
+                pd = pd > kMaxParts ? kMaxParts : pd;
+                qi.parts = (uint16_t)pd;
+                list = small ? kListDenseSmall : kListDenseWide;
+            }
+        }
+        W.qinfo[q] = qi;
+        W.done[q] = 0;
+        W.qstate[q] = 0;
+        if (list >= 0) {
+            uint2 *wl = W.work + (size_t)list * W.work_stride;
+            uint32_t base = atomicAdd(&W.ctr[2 * list], (uint32_t)qi.parts);
+            for (uint32_t p = 0; p < qi.parts; ++p) wl[base + p] = make_uint2((uint32_t)q, p);
+        }
+    }
+    // queries without any matching posting: padded results right away
+    __syncwarp();
+    if (k >= 1 && k <= (uint32_t)kMaxK && total == 0) {
+        const int64_t o = Q.out_off[q];
+        for (uint32_t j = lane; j < k; j += 32) {
+            W.out_ids[o + j] = 0;
+            W.out_counts[o + j] = 0;
+            if (W.out_scores) W.out_scores[o + j] = 0.0f;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ shared
+
+// Items of one query part staged in shared memory.
+struct ItemStage {
+    int64_t *start;   // [kItemChunk] global position of the sub-span
+    uint32_t *len;    // [kItemChunk]
+    uint32_t *inc;    // [kItemChunk]
+    uint32_t *flat;   // [kItemChunk+1] exclusive prefix of len
+};
+
+// Stream every posting id of the staged sub-spans through `visit(id, inc)`.
+// Warps take 256-position chunks of the flattened span list; each lane loads
+// 8 ids (coalesced within a span) before visiting them.
+template <class V>
+__device__ __forceinline__ void stream_ids(const uint32_t *__restrict__ ids, const ItemStage &st,
+                                           uint32_t n_items, uint32_t F, V &&visit) {
+    const uint32_t lane = lane_id();
+    const uint32_t nw = blockDim.x >> 5;
+    for (uint32_t base = warp_id() * 256u; base < F; base += nw * 256u) {
+        uint32_t it = 0;
+        if (lane == 0) {
+            uint32_t lo = 0, hi = n_items;       // last item with flat <= base
+            while (lo < hi) {
+                uint32_t mid = (lo + hi + 1) >> 1;
+                if (st.flat[mid] <= base) lo = mid; else hi = mid - 1;
+            }
+            it = lo;
+        }
+        it = __shfl_sync(0xffffffffu, it, 0);
+        uint32_t v[8], inc[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            uint32_t f = base + j * 32 + lane;
+            inc[j] = 0;
+            v[j] = 0;
+            if (f < F) {
+                while (st.flat[it + 1] <= f) ++it;
+                int64_t pos = st.start[it] + (int64_t)(f - st.flat[it]);
+                v[j] = __ldg(ids + pos);
+                inc[j] = st.inc[it];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (inc[j]) visit(v[j], inc[j]);
+    }
+}
+
+// Scratch / merge of a query's parts.  Part p of query q keeps its sorted
+// top-k keys in scratch[out_off*kMaxParts + p*k ..].
+struct MergeSet {
+    const uint64_t *keys;
+    const uint32_t *cnt;
+    uint32_t parts, k;
+    template <class F>
+    __device__ void for_each(F f) const {
+        for (uint32_t p = 0; p < parts; ++p) {
+            const uint32_t n = __ldcg(cnt + p);
+            for (uint32_t b = 0; b < n; b += blockDim.x) {
+                uint32_t i = b + threadIdx.x;
+                bool act = i < n;
+                uint64_t key = act ? __ldcg(keys + (size_t)p * k + i) : 0ull;
+                f(act, key_prim(key), key_id(key));
+            }
+        }
+    }
+};
+
+__device__ void convert_to_dense(const DevIndex &ix, const Work &W, const Tuning &T, uint32_t q) {
+    QInfo qi = W.qinfo[q];
+    const bool small = (qi.flags & kFlagSmallCount) != 0;
+    const int64_t tile = small ? T.dense_tile_u8 : T.dense_tile_u32;
+    const int64_t ntiles = (ix.n_objects + tile - 1) / tile;
+    int64_t pd = (qi.total + T.dense_part_work - 1) / T.dense_part_work;
+    pd = pd < 1 ? 1 : pd;
+    pd = pd > ntiles ? ntiles : pd;
+    pd = pd > kMaxParts ? kMaxParts : pd;
+    qi.parts = (uint16_t)pd;
+    qi.cls = kClsDense;
+    W.qinfo[q] = qi;
+    W.done[q] = 0;
+    const int list = small ? kListDenseSmall : kListDenseWide;
+    uint2 *wl = W.work + (size_t)list * W.work_stride;
+    uint32_t base = atomicAdd(&W.ctr[2 * list], (uint32_t)pd);
+    for (uint32_t p = 0; p < pd; ++p) wl[base + p] = make_uint2(q, p);
+}
+
+// Finish one part: publish its keys, and let the last part merge them.
+__device__ void finish_part(const DevIndex &ix, const Work &W, const Tuning &T, const DevQueries &Q,
+                            uint32_t q, uint32_t p, const QInfo &qi, uint64_t *cand, uint32_t n,
+                            SelectScratch &ss, bool failed) {
+    const int64_t out_off = Q.out_off[q];
+    const bool weighted = (qi.flags & kFlagWeighted) != 0;
+    if (qi.parts == 1 && !failed) {
+        write_results(W, out_off, qi.k, cand, n, weighted, qi.scale);
+        return;
+    }
+    uint64_t *dst = W.scratch + (size_t)out_off * kMaxParts + (size_t)p * qi.k;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) __stcg(dst + i, cand[i]);
+    if (threadIdx.x == 0) {
+        __stcg(W.part_cnt + (size_t)q * kMaxParts + p, failed ? 0u : n);
+        if (failed) atomicOr(&W.qstate[q], 1u);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t prev = atomicAdd(&W.done[q], 1u);
+        ss.sc[12] = (prev == (uint32_t)qi.parts - 1) ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!ss.sc[12]) return;
+    __threadfence();
+    if (atomicAdd(&W.qstate[q], 0u) & 1u) {       // a sparse part overflowed: redo densely
+        if (threadIdx.x == 0) convert_to_dense(ix, W, T, q);
+        __syncthreads();
+        return;
+    }
+    MergeSet ms{W.scratch + (size_t)out_off * kMaxParts, W.part_cnt + (size_t)q * kMaxParts,
+                qi.parts, qi.k};
+    const int bits = (qi.flags & kFlagSmallCount) ? 8 : 32;
+    uint32_t nn = select_topk(ms, qi.k, bits, cand, kCandCap, ss);
+    write_results(W, out_off, qi.k, cand, nn, weighted, qi.scale);
+    __syncthreads();
+    if (threadIdx.x == 0) W.done[q] = 0;
+}
+
+// ------------------------------------------------------------------ sparse
+
+__device__ __forceinline__ uint32_t slot_of(uint32_t id, uint32_t cap) {
+    return (uint32_t)(((uint64_t)(id * 0x9E3779B1u) * cap) >> 32);
+}
+
+template <bool PACKED>
+struct HashSet {
+    const void *tab;
+    uint32_t cap;
+    template <class F>
+    __device__ void for_each(F f) const {
+        for (uint32_t b = 0; b < cap; b += blockDim.x) {
+            uint32_t i = b + threadIdx.x;
+            bool act = i < cap;
+            uint32_t prim = 0, id = 0;
+            if (PACKED) {
+                uint32_t v = act ? ((const uint32_t *)tab)[i] : 0u;
+                act = act && v != 0;
+                prim = v & 255u;
+                id = v >> 8;
+            } else {
+                uint64_t v = act ? ((const uint64_t *)tab)[i] : 0ull;
+                act = act && v != 0;
+                prim = (uint32_t)v;
+                id = (uint32_t)(v >> 32) - 1u;
+            }
+            f(act, prim, id);
+        }
+    }
+};
+
+// Per-part hash of object id -> count (or fixed-point weight sum) in shared
+// memory; replaces the per-query bitmap + c-PQ (match_device_utils.h:160-446).
+template <bool PACKED>
+__global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t tid = threadIdx.x;
+    const uint32_t slots_max = PACKED ? (uint32_t)T.sparse_slots_packed : (uint32_t)T.sparse_slots_wide;
+    const size_t tab_bytes = (size_t)slots_max * (PACKED ? 4 : 8);
+    unsigned char *tab_raw = smem;
+    unsigned char *uni = smem + tab_bytes;                      // items | candidates
+    ItemStage st;
+    st.start = (int64_t *)uni;
+    st.len = (uint32_t *)(uni + kItemChunk * 8);
+    st.inc = (uint32_t *)(uni + kItemChunk * 12);
+    st.flat = (uint32_t *)(uni + kItemChunk * 16);
+    uint64_t *cand = (uint64_t *)uni;
+    SelectScratch &ss = *(SelectScratch *)(uni + kCandCap * 8);
+    __shared__ uint32_t s_work;
+
+    const int list = PACKED ? kListSparsePacked : kListSparseWide;
+    for (;;) {
+        if (tid == 0) s_work = atomicAdd(&W.ctr[2 * list + 1], 1u);
+        __syncthreads();
+        const uint32_t w = s_work;
+        __syncthreads();
+        if (w >= *(volatile uint32_t *)&W.ctr[2 * list]) break;
+        const uint2 wk = W.work[(size_t)list * W.work_stride + w];
+        const uint32_t q = wk.x, p = wk.y;
+        const QInfo qi = W.qinfo[q];
+        const uint32_t P = qi.parts;
+        const uint32_t id_lo = (uint32_t)(((uint64_t)ix.n_objects * p) / P);
+        const uint32_t id_hi = (uint32_t)(((uint64_t)ix.n_objects * (p + 1)) / P);
+
+        // pass 1: part size (sum of sub-span lengths) bounds the distinct ids
+        uint64_t part_total = 0;
+        for (int32_t c0 = 0; c0 < qi.n_items; c0 += kItemChunk) {
+            const int32_t mc = min(kItemChunk, qi.n_items - c0);
+            uint32_t len = 0;
+            if ((int32_t)tid < mc) {
+                const int64_t it = qi.item0 + c0 + tid;
+                const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
+                int64_t a = s0, b = e0;
+                if (P > 1 && e0 > s0) {
+                    a = p == 0 ? s0 : lower_bound_u32(ix.ids, s0, e0, id_lo);
+                    b = p == P - 1 ? e0 : lower_bound_u32(ix.ids, a, e0, id_hi);
+                }
+                st.start[tid] = a;
+                st.inc[tid] = W.inc[it];
+                len = (uint32_t)(b - a);
+                st.len[tid] = len;
+            }
+            uint32_t tot = 0;
+            uint32_t off = block_excl_scan(len, ss.tmp, &tot);
+            if ((int32_t)tid < mc) st.flat[tid] = off;
+            if (tid == 0) st.flat[mc] = tot;
+            part_total += tot;
+            if (qi.n_items > kItemChunk) __syncthreads();
+        }
+        const bool single = qi.n_items <= kItemChunk;
+        const bool overflow = part_total > (uint64_t)slots_max * 3 / 4;
+        uint64_t *cand_out = cand;
+        uint32_t nres = 0;
+        if (!overflow) {
+            uint32_t cap = (uint32_t)umin64((uint64_t)slots_max, part_total + part_total / 3 + 64);
+            cap = (cap + 31) & ~31u;
+            if (cap > slots_max) cap = slots_max;
+            // zero the table
+            uint4 *t4 = (uint4 *)tab_raw;
+            const uint32_t n4 = (cap * (PACKED ? 4 : 8) + 15) / 16;
+            for (uint32_t i = tid; i < n4; i += blockDim.x) t4[i] = make_uint4(0, 0, 0, 0);
+            __syncthreads();
+            for (int32_t c0 = 0; c0 < qi.n_items; c0 += kItemChunk) {
+                const int32_t mc = min(kItemChunk, qi.n_items - c0);
+                if (!single) {        // restage this chunk (pass 1 kept only the last)
+                    uint32_t len = 0;
+                    if ((int32_t)tid < mc) {
+                        const int64_t it = qi.item0 + c0 + tid;
+                        const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
+                        int64_t a = s0, b = e0;
+                        if (P > 1 && e0 > s0) {
+                            a = p == 0 ? s0 : lower_bound_u32(ix.ids, s0, e0, id_lo);
+                            b = p == P - 1 ? e0 : lower_bound_u32(ix.ids, a, e0, id_hi);
+                        }
+                        st.start[tid] = a;
+                        st.inc[tid] = W.inc[it];
+                        len = (uint32_t)(b - a);
+                    }
+                    uint32_t tot = 0;
+                    uint32_t off = block_excl_scan(len, ss.tmp, &tot);
+                    if ((int32_t)tid < mc) st.flat[tid] = off;
+                    if (tid == 0) st.flat[mc] = tot;
+                    __syncthreads();
+                } else {
+                    __syncthreads();
+                }
+                const uint32_t F = st.flat[mc];
+                if (PACKED) {
+                    uint32_t *tab = (uint32_t *)tab_raw;
+                    stream_ids(ix.ids, st, (uint32_t)mc, F, [&](uint32_t id, uint32_t) {
+                        uint32_t h = slot_of(id, cap);
+                        const uint32_t want = (id << 8) | 1u;
+                        for (uint32_t probe = 0; probe < cap; ++probe) {
+                            uint32_t cur = tab[h];
+                            if (cur == 0u) {
+                                uint32_t old = atomicCAS(&tab[h], 0u, want);
+                                if (old == 0u) return;
+                                cur = old;
+                            }
+                            if ((cur >> 8) == id) { atomicAdd(&tab[h], 1u); return; }
+                            h = (h + 1 == cap) ? 0 : h + 1;
+                        }
+                    });
+                } else {
+                    unsigned long long *tab = (unsigned long long *)tab_raw;
+                    stream_ids(ix.ids, st, (uint32_t)mc, F, [&](uint32_t id, uint32_t inc) {
+                        uint32_t h = slot_of(id, cap);
+                        const unsigned long long tag = (unsigned long long)(id + 1u) << 32;
+                        for (uint32_t probe = 0; probe < cap; ++probe) {
+                            unsigned long long cur = tab[h];
+                            if (cur == 0ull) {
+                                unsigned long long old = atomicCAS(&tab[h], 0ull, tag | inc);
+                                if (old == 0ull) return;
+                                cur = old;
+                            }
+                            if ((cur & 0xFFFFFFFF00000000ull) == tag) {
+                                atomicAdd(&tab[h], (unsigned long long)inc);
+                                return;
+                            }
+                            h = (h + 1 == cap) ? 0 : h + 1;
+                        }
+                    });
+                }
+                __syncthreads();
+            }
+            HashSet<PACKED> hs{tab_raw, cap};
+            const int bits = PACKED ? 8 : 32;
+            nres = select_topk(hs, qi.k, bits, cand_out, kCandCap, ss);
+        }
+        finish_part(ix, W, T, Q, q, p, qi, cand_out, nres, ss, overflow);
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ dense
+
+template <bool SMALL>
+struct TileSet {
+    const uint32_t *cnt;     // counters (bytes packed 4 per word when SMALL)
+    uint32_t n_ids;          // ids in this tile (multiple of 16 when SMALL)
+    uint32_t tile_lo;
+    uint32_t thr;            // admit primaries > thr
+    const uint64_t *S;
+    uint32_t nS;
+    template <class F>
+    __device__ void for_each(F f) const {
+        for (uint32_t b = 0; b < nS; b += blockDim.x) {
+            uint32_t i = b + threadIdx.x;
+            bool act = i < nS;
+            uint64_t key = act ? S[i] : 0ull;
+            f(act, key_prim(key), key_id(key));
+        }
+        const uint32_t per = SMALL ? 16u : 4u;
+        const uint32_t nvec = (n_ids + per - 1) / per;
+        const uint32_t thr4 = SMALL ? thr * 0x01010101u : thr;
+        for (uint32_t b = 0; b < nvec; b += blockDim.x) {
+            uint32_t v = b + threadIdx.x;
+            bool act = v < nvec;
+            uint4 w = act ? ((const uint4 *)cnt)[v] : make_uint4(0, 0, 0, 0);
+            bool any;
+            if (SMALL)
+                any = (__vcmpgtu4(w.x, thr4) | __vcmpgtu4(w.y, thr4) | __vcmpgtu4(w.z, thr4) |
+                       __vcmpgtu4(w.w, thr4)) != 0u;
+            else
+                any = w.x > thr || w.y > thr || w.z > thr || w.w > thr;
+            if (__ballot_sync(0xffffffffu, act && any) == 0u) continue;
+            const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (uint32_t e = 0; e < per; ++e) {
+                uint32_t prim = SMALL ? ((words[e >> 2] >> ((e & 3) * 8)) & 255u) : words[e];
+                uint32_t local = v * per + e;
+                f(act && prim > thr && local < n_ids, prim, tile_lo + local);
+            }
+        }
+    }
+};
+
+// Id-tiled dense counters in shared memory; one CTA sweeps the tiles of one
+// query part, keeping its running top-k.  Replaces the per-query global bitmap
+// (match.cu:276-294, match_device_utils.h:422-446), which wraps above
+// 2^bits - 1; these counters are sized from the item count and never wrap.
+template <bool SMALL>
+__global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const uint32_t tid = threadIdx.x;
+    const uint32_t tile_cap = SMALL ? (uint32_t)T.dense_tile_u8 : (uint32_t)T.dense_tile_u32;
+    const size_t cnt_bytes = (size_t)tile_cap * (SMALL ? 1 : 4);
+    uint32_t *cnt = (uint32_t *)smem;
+    uint64_t *S = (uint64_t *)(smem + cnt_bytes);
+    uint64_t *cand = S + kMaxK;
+    unsigned char *it_raw = (unsigned char *)(cand + kCandCap);
+    int64_t *cur = (int64_t *)it_raw;
+    ItemStage st;
+    st.start = (int64_t *)(it_raw + kItemChunk * 8);
+    st.len = (uint32_t *)(it_raw + kItemChunk * 16);
+    st.inc = (uint32_t *)(it_raw + kItemChunk * 20);
+    st.flat = (uint32_t *)(it_raw + kItemChunk * 24);
+    SelectScratch &ss = *(SelectScratch *)(it_raw + kItemChunk * 28 + 16);
+    __shared__ uint32_t s_work, s_nS;
+
+    const int list = SMALL ? kListDenseSmall : kListDenseWide;
+    for (;;) {
+        if (tid == 0) s_work = atomicAdd(&W.ctr[2 * list + 1], 1u);
+        __syncthreads();
+        const uint32_t w = s_work;
+        __syncthreads();
+        if (w >= *(volatile uint32_t *)&W.ctr[2 * list]) break;
+        const uint2 wk = W.work[(size_t)list * W.work_stride + w];
+        const uint32_t q = wk.x, p = wk.y;
+        const QInfo qi = W.qinfo[q];
+        const uint32_t P = qi.parts;
+        const uint64_t N = (uint64_t)ix.n_objects;
+        const uint64_t ntiles = (N + tile_cap - 1) / tile_cap;
+        const uint64_t t0 = ntiles * p / P, t1 = ntiles * (p + 1) / P;
+        const bool single = qi.n_items <= kItemChunk;
+        const bool weighted = (qi.flags & kFlagWeighted) != 0;
+        if (tid == 0) s_nS = 0;
+        // cursor of every item at the part's first id
+        if (single && (int32_t)tid < qi.n_items) {
+            const int64_t it = qi.item0 + tid;
+            const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
+            cur[tid] = (t0 == 0 || e0 == s0) ? s0
+                                             : lower_bound_u32(ix.ids, s0, e0, (uint32_t)(t0 * tile_cap));
+        }
+        __syncthreads();
+        for (uint64_t t = t0; t < t1; ++t) {
+            const uint32_t tile_lo = (uint32_t)(t * tile_cap);
+            const uint32_t tile_hi = (uint32_t)umin64(N, (t + 1) * tile_cap);
+            const uint32_t n_ids = tile_hi - tile_lo;
+            const uint32_t n_pad = (n_ids + 15) & ~15u;
+            // zero the counters of this tile
+            uint4 *c4 = (uint4 *)cnt;
+            const uint32_t n4 = (n_pad * (SMALL ? 1 : 4)) / 16;
+            for (uint32_t i = tid; i < n4; i += blockDim.x) c4[i] = make_uint4(0, 0, 0, 0);
+            bool any_ids = false;
+            for (int32_t c0 = 0; c0 < qi.n_items; c0 += kItemChunk) {
+                const int32_t mc = min(kItemChunk, qi.n_items - c0);
+                uint32_t len = 0;
+                if ((int32_t)tid < mc) {
+                    const int64_t it = qi.item0 + c0 + tid;
+                    const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
+                    int64_t a = single ? cur[tid] : (t == 0 ? s0 : lower_bound_u32(ix.ids, s0, e0, tile_lo));
+                    int64_t b = (tile_hi >= N) ? e0 : gallop_u32(ix.ids, a, e0, tile_hi);
+                    st.start[tid] = a;
+                    st.inc[tid] = W.inc[it];
+                    len = (uint32_t)(b - a);
+                    if (single) cur[tid] = b;
+                }
+                uint32_t tot = 0;
+                uint32_t off = block_excl_scan(len, ss.tmp, &tot);
+                if ((int32_t)tid < mc) st.flat[tid] = off;
+                if (tid == 0) st.flat[mc] = tot;
+                __syncthreads();
+                if (tot) any_ids = true;
+                if (SMALL) {
+                    stream_ids(ix.ids, st, (uint32_t)mc, tot, [&](uint32_t id, uint32_t) {
+                        const uint32_t loc = id - tile_lo;
+                        atomicAdd(&cnt[loc >> 2], 1u << ((loc & 3u) << 3));
+                    });
+                } else {
+                    stream_ids(ix.ids, st, (uint32_t)mc, tot, [&](uint32_t id, uint32_t inc) {
+                        atomicAdd(&cnt[id - tile_lo], inc);
+                    });
+                }
+                __syncthreads();
+            }
+            if (!any_ids) continue;
+            // merge this tile into the running top-k
+            const uint32_t nS = s_nS;
+            const uint32_t thr = nS == qi.k ? key_prim(S[qi.k - 1]) : 0u;
+            TileSet<SMALL> ts{cnt, n_ids, tile_lo, thr, S, nS};
+            const uint32_t nn = select_topk(ts, qi.k, SMALL ? 8 : 32, cand, kCandCap, ss);
+            for (uint32_t i = tid; i < nn; i += blockDim.x) S[i] = cand[i];
+            if (tid == 0) s_nS = nn;
+            __syncthreads();
+        }
+        const uint32_t nS = s_nS;
+        for (uint32_t i = tid; i < nS; i += blockDim.x) cand[i] = S[i];
+        __syncthreads();
+        (void)weighted;
+        finish_part(ix, W, T, Q, q, p, qi, cand, nS, ss, false);
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+size_t sparse_smem_bytes(const Tuning &t, bool packed) {
+    size_t tab = (size_t)(packed ? t.sparse_slots_packed * 4 : t.sparse_slots_wide * 8);
+    size_t uni = std::max<size_t>(kItemChunk * 20 + 16, kCandCap * 8);
+    return tab + uni + sizeof(SelectScratch) + 64;
+}
+
+size_t dense_smem_bytes(const Tuning &t, bool small) {
+    size_t c = (size_t)(small ? t.dense_tile_u8 : t.dense_tile_u32 * 4);
+    return c + (size_t)kMaxK * 8 + (size_t)kCandCap * 8 + kItemChunk * 28 + 16 + sizeof(SelectScratch) + 64;
+}
+
+Tuning default_tuning() {
+    Tuning t;
+    t.sparse_slots_packed = 22528;   // 88 KiB of 4-byte slots: two CTAs per SM
+    t.sparse_slots_wide = 11264;     // 88 KiB of 8-byte slots
+    t.sparse_threads = 512;
+    t.dense_tile_u8 = 147456;        // 144 KiB of 1-byte counters
+    t.dense_tile_u32 = 36864;        // 144 KiB of 4-byte counters
+    t.dense_threads = 1024;
+    t.sparse_max_total = 16 * 16896;
+    t.dense_part_work = 4 << 20;
+    t.sparse_ctas_per_sm = 2;
+    t.dense_ctas_per_sm = 1;
+    return t;
+}
+
+static cudaError_t set_smem(const void *fn, size_t bytes) {
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+cudaError_t prepare_kernels(const Tuning &t) {
+    cudaError_t e;
+    if ((e = set_smem((const void *)k_sparse<true>, sparse_smem_bytes(t, true)))) return e;
+    if ((e = set_smem((const void *)k_sparse<false>, sparse_smem_bytes(t, false)))) return e;
+    if ((e = set_smem((const void *)k_dense<true>, dense_smem_bytes(t, true)))) return e;
+    if ((e = set_smem((const void *)k_dense<false>, dense_smem_bytes(t, false)))) return e;
+    return cudaSuccess;
+}
+
+cudaError_t prepare_kernels_max() {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (optin <= 0) optin = 227 * 1024;
+    cudaError_t e;
+    if ((e = set_smem((const void *)k_sparse<true>, optin))) return e;
+    if ((e = set_smem((const void *)k_sparse<false>, optin))) return e;
+    if ((e = set_smem((const void *)k_dense<true>, optin))) return e;
+    if ((e = set_smem((const void *)k_dense<false>, optin))) return e;
+    return cudaSuccess;
+}
+
+int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t,
+                 int num_sms, cudaStream_t s) {
+    if (Q.n_queries <= 0) return 0;
+    int launches = 0;
+    cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), s);
+    const int plan_blocks = (int)((Q.n_queries * 32LL + 255) / 256);
+    k_plan<<<plan_blocks, 256, 0, s>>>(ix, Q, W, t);
+    ++launches;
+    const int sg = num_sms * std::max(1, t.sparse_ctas_per_sm);
+    k_sparse<true><<<sg, t.sparse_threads, sparse_smem_bytes(t, true), s>>>(ix, Q, W, t);
+    k_sparse<false><<<sg, t.sparse_threads, sparse_smem_bytes(t, false), s>>>(ix, Q, W, t);
+    const int dg = num_sms * std::max(1, t.dense_ctas_per_sm);
+    k_dense<true><<<dg, t.dense_threads, dense_smem_bytes(t, true), s>>>(ix, Q, W, t);
+    k_dense<false><<<dg, t.dense_threads, dense_smem_bytes(t, false), s>>>(ix, Q, W, t);
+    launches += 4;
+    return launches;
+}
+
+}  // namespace gg

@@ -1,0 +1,22 @@
+// match.cuh -- host-side entry points of the match path (match.cu).
+#pragma once
+#include "device.cuh"
+
+#include <cstddef>
+
+namespace gg {
+
+Tuning default_tuning();
+size_t sparse_smem_bytes(const Tuning &t, bool packed);
+size_t dense_smem_bytes(const Tuning &t, bool small);
+cudaError_t prepare_kernels(const Tuning &t);
+// Allow the largest dynamic shared memory on every match kernel (once per device).
+cudaError_t prepare_kernels_max();
+
+// Enqueue plan + sparse + dense kernels for one batch on stream s.  All
+// pointers in Q and W are device pointers; W arrays are sized for Q.
+// Returns the number of kernel launches issued.
+int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t,
+                 int num_sms, cudaStream_t s);
+
+}  // namespace gg

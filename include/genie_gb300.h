@@ -1,0 +1,219 @@
+/*
+ * genie_gb300.h -- C ABI of the GB300-native GENIE match-count top-k search.
+ *
+ * This is the drop-in boundary: plain pointers and sizes, opaque handles,
+ * int status codes.  The C++ first/second-level interface (include/genie/)
+ * and the Python mirror (genie_gb300/) are thin callers of these entry
+ * points.  Each declaration names the reference interface it replaces.
+ *
+ * Results: query q owns k[q] slots starting at out_off[q] = sum_{p<q} k[p]
+ * (q*k for a uniform k, the reference's row-major layout, knn.cu:165-175).
+ * Slots are sorted by (primary desc, id asc); primary is the match count of
+ * an unweighted query, or the exact fixed-point sum of matched item weights
+ * of a weighted one.  Slots beyond the objects with a non-zero primary hold
+ * (id 0, count 0, score 0), as the reference pads (heap_count.cu:254-255).
+ *
+ * Thread safety: an index handle is immutable after creation and may be
+ * searched from several threads; a batch or server handle has one owner.
+ */
+#ifndef GENIE_GB300_H_
+#define GENIE_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The C++ shim maps them back to the reference's exception
+ * types (src/genie/exception/exception.h:10-46). */
+enum genie_status {
+    GENIE_OK = 0,
+    GENIE_ERR_INVALID_ARG = 1,      /* InvalidConfigurationException / cpu_runtime_error */
+    GENIE_ERR_GPU_ALLOC = 2,        /* gpu_bad_alloc */
+    GENIE_ERR_CUDA = 3,             /* gpu_runtime_error */
+    GENIE_ERR_NOT_IMPLEMENTED = 4,  /* NotImplementedException */
+    GENIE_ERR_CPU_ALLOC = 5,        /* cpu_bad_alloc */
+    GENIE_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device wait ran out */
+    GENIE_ERR_IO = 7,               /* file could not be read or written */
+    GENIE_ERR_ADMISSION = 8         /* server: request exceeds the memory budget */
+};
+
+/* Codec ids: the reference COMPRESSION_TYPE enum (DeviceCodecFactory.h:38-53). */
+enum genie_codec {
+    GENIE_NO_COMPRESSION = 0, GENIE_COPY, GENIE_DELTA, GENIE_BP32, GENIE_VARINT,
+    GENIE_COMP_BP32_COPY, GENIE_COMP_BP32_VARINT, GENIE_SERIAL_COPY_COPY,
+    GENIE_SERIAL_DELTA_COPY, GENIE_SERIAL_DELTA_DELTA, GENIE_SERIAL_DELTA_VARINT,
+    GENIE_SERIAL_DELTA_BP32, GENIE_SERIAL_DELTA_COMP_BP32_COPY,
+    GENIE_SERIAL_DELTA_COMP_BP32_VARINT, GENIE_N_CODECS
+};
+
+typedef struct genie_index genie_index;
+typedef struct genie_batch genie_batch;
+typedef struct genie_server genie_server;
+
+/* Message of the last failed call on this thread (never NULL). */
+const char *genie_last_error(void);
+/* ABI version (major*10000 + minor*100 + patch). */
+int genie_version(void);
+
+/* Select and initialise a device.  Replaces genie::utility::Init /
+ * init_genie (src/genie/utility/init.cu:7-34). */
+int genie_init(int device);
+
+/* ---------------------------------------------------------------- index */
+
+typedef struct {
+    int64_t n_objects;     /* inv_table::i_size (inv_table.cu:93-96) */
+    int32_t n_dims;        /* inv_table::m_size (inv_table.cu:87-91) */
+    int32_t codec;         /* genie_codec; 0 = uncompressed */
+    int64_t n_ids;         /* posting entries (inv_table::inv()->size()) */
+    int64_t n_keys;        /* (dim, value) lists */
+    int64_t n_words;       /* compressed words (0 when uncompressed) */
+    int64_t n_segments;    /* compressed segments (0 when uncompressed) */
+    int32_t max_multiplicity; /* most times one id repeats in one list */
+    int32_t max_segment;   /* segment length bound of a compressed index */
+    int64_t device_bytes;  /* HBM held by the index */
+} genie_index_info;
+
+/* Build a resident index from a row-major n_objects x n_dims value matrix.
+ * Replaces preprocess_for_knn_csv + load_table + inv_table::build +
+ * inv_table::cpy_data_to_gpu (original/interface.cc:150-353,
+ * table/inv_table.cu:267-350, table/inv_table.cu:30-45). */
+int genie_index_create(const int32_t *values, int64_t n_objects, int32_t n_dims,
+                       genie_index **out);
+
+/* Single-dim "bag" index (every value of row r lists r).  Replaces
+ * load_table_bijectMap (original/interface.cc:621-646, inv_list.cc:51-84). */
+int genie_index_create_bag(const int32_t *values, const int64_t *row_off,
+                           int64_t n_objects, genie_index **out);
+
+/* Compressed index: each (dim,value) list is cut into segments of at most
+ * max_segment ids (<= 1024) and every segment is encoded with `codec`.
+ * Replaces inv_compr_table::build (table/inv_compr_table.cu:30-119). */
+int genie_index_create_compressed(const int32_t *values, int64_t n_objects, int32_t n_dims,
+                                  int32_t codec, int32_t max_segment, genie_index **out);
+
+int genie_index_destroy(genie_index *ix);
+int genie_index_get_info(const genie_index *ix, genie_index_info *out);
+
+/* Copy the index back to the host (any pointer may be NULL).  ids holds the
+ * device posting array, which equals the reference's inv_table::inv()
+ * (test_save2gpu_sift.cc:91-100).  key_offsets has n_keys+1 entries, the
+ * per-dim arrays n_dims entries, key_base n_dims+1 entries. */
+int genie_index_copy_out(const genie_index *ix, uint32_t *ids, int64_t *key_offsets,
+                         int64_t *key_base, int32_t *dim_min, int32_t *dim_max);
+
+/* Copy the compressed layout back (any pointer may be NULL): words[n_words],
+ * key_seg[n_keys+1], seg_word_off[n_segments+1], seg_first/seg_len[n_segments]. */
+int genie_index_copy_compressed(const genie_index *ix, uint32_t *words, int64_t *key_seg,
+                                int64_t *seg_word_off, uint32_t *seg_first, uint32_t *seg_len);
+
+/* Span [start,end) of one query item in the posting array; 0 length when the
+ * item matches nothing.  Replaces Query::build (query/query.cc:273-333). */
+int genie_index_item_span(const genie_index *ix, int32_t dim, int32_t low, int32_t up,
+                          int64_t *start, int64_t *end);
+
+/* Widen [low,up] until the covered lists hold ceil(sel*N) ids.  Replaces
+ * Query::apply_adaptive_query_range (query/query.cc:196-261). */
+int genie_index_adaptive_range(const genie_index *ix, int32_t dim, float selectivity,
+                               int32_t *low, int32_t *up);
+
+/* Save / load an index in this library's own versioned file format
+ * (header + arrays + checksum).  Replaces SaveTableToBinary /
+ * LoadTableFromBinary (interface/io.h:16-28, utility/serialization.cc:23-58). */
+int genie_index_save(const genie_index *ix, const char *path);
+int genie_index_load(const char *path, genie_index **out);
+
+/* ---------------------------------------------------------------- search */
+
+/* A batch of queries.  Query q owns items [item_off[q], item_off[q+1]);
+ * item i matches dim[i] with values in [low[i], up[i]] (inclusive).
+ * weight/weighted may be NULL: a query is weighted when weighted[q] != 0,
+ * and then every weight of its items must be finite and > 0.  k may be NULL,
+ * in which case every query uses uniform_k.  Mirrors Query::range
+ * (query/query.h:43-54) and knn_search's topk (knn.cu:158-159). */
+typedef struct {
+    int32_t n_queries;
+    const int64_t *item_off;
+    const int32_t *dim;
+    const int32_t *low;
+    const int32_t *up;
+    const float *weight;
+    const uint8_t *weighted;
+    const uint32_t *k;
+    uint32_t uniform_k;
+} genie_queries;
+
+/* Plain per-batch search from host buffers to host buffers: query upload,
+ * match, top-k, result download, synchronous.  Replaces
+ * original::knn_search(table, queries, h_topk, h_topk_count, config)
+ * (original/interface.cc:826-857) and matching::knn (knn.cu:106-183).
+ * scores may be NULL. */
+int genie_search(genie_index *ix, const genie_queries *q, uint32_t *out_ids,
+                 uint32_t *out_counts, float *out_scores);
+
+/* Multi-index search, one query batch per index, results concatenated in
+ * index order.  Replaces knn_search_MT / knn_MT
+ * (original/interface.cc:859-909, matching/knn.cu:185-283). */
+int genie_search_multi(genie_index *const *ix, const genie_queries *q, int32_t n_index,
+                       uint32_t *out_ids, uint32_t *out_counts, float *out_scores);
+
+/* Search with every pointer in device memory on the given cudaStream_t
+ * (NULL = the legacy default stream); asynchronous. */
+int genie_search_device(genie_index *ix, const genie_queries *q_dev, const int64_t *out_off_dev,
+                        uint32_t *out_ids, uint32_t *out_counts, float *out_scores,
+                        void *stream);
+
+/* ---------------------------------------------------------------- batched */
+
+typedef struct {
+    int32_t max_queries;     /* capacity of one run */
+    int64_t max_items;
+    uint32_t max_k;
+    int32_t use_graph;       /* capture the run as one CUDA graph */
+    int32_t autotune;        /* pick tile/table sizes by timing candidates */
+} genie_batch_config;
+
+typedef struct {
+    int32_t sparse_parts_cap;   /* hash slots per CTA */
+    int32_t sparse_threads;
+    int32_t dense_tile;         /* ids per dense tile */
+    int32_t dense_threads;
+    int64_t sparse_max_total;   /* queries touching more ids go dense */
+    int64_t dense_part_work;    /* ids per dense part */
+} genie_tuning;
+
+/* Batched search: fixed-capacity device buffers, device-side query compile,
+ * persistent match kernels, optional CUDA-graph capture and autotuning. */
+int genie_batch_create(genie_index *ix, const genie_batch_config *cfg, genie_batch **out);
+int genie_batch_destroy(genie_batch *b);
+int genie_batch_run(genie_batch *b, const genie_queries *q, uint32_t *out_ids,
+                    uint32_t *out_counts, float *out_scores);
+/* Tune on a sample batch (timing on the device), then keep the winner. */
+int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuning *chosen);
+int genie_batch_get_tuning(const genie_batch *b, genie_tuning *out);
+int genie_batch_set_tuning(genie_batch *b, const genie_tuning *t);
+/* Launch statistics of the last run: kernels launched, device milliseconds. */
+int genie_batch_last_stats(const genie_batch *b, int32_t *kernels, float *device_ms);
+
+/* ---------------------------------------------------------------- codecs */
+
+/* Host encoder of the reference byte formats (DeviceCodecFactory.cu:13-48).
+ * Returns words written or a negative status. */
+int64_t genie_codec_encode(int32_t codec, const uint32_t *in, int64_t n, uint32_t *out, int64_t cap);
+/* Worst-case words genie_codec_encode may write for n values. */
+int64_t genie_codec_encode_bound(int64_t n);
+/* Device decode of independent encoded segments: segment s spans words
+ * [word_off[s], word_off[s+1]) and decodes to out[out_off[s] ..).  All
+ * pointers are device pointers; out_len[s] receives each decoded length.
+ * Replaces g_decodeArrayParallel (DeviceCodecTemplatesImpl.hpp:4-34). */
+int genie_codec_decode_device(int32_t codec, const uint32_t *words, const int64_t *word_off,
+                              int64_t n_segments, const int64_t *out_off, uint32_t *out,
+                              uint32_t *out_len, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
