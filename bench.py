@@ -1,0 +1,337 @@
+#!/usr/bin/env python
+"""Benchmark of GB300-native GENIE match-count top-k search.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one batch of the LSH-style workload (1,000,000 objects x 240 dims,
+bucket ids uniform in [0, 8192), 1,024 queries of 240 exact items, half of
+them derived from stored objects with 60% of items redrawn, k = 100) searched
+to exact top-k.  Prints one JSON line:
+
+  value      queries/s with the batch resident in HBM: the captured CUDA graph
+             (device-side query compile + persistent match kernels + top-k),
+             CUDA events on the launching stream, L2 flushed before every step
+  e2e        queries/s through genie_batch_run from host buffers: pinned H2D of
+             the queries, the graph, D2H of ids/counts, per step
+  roofline   posting-list bytes touched per launch / the dominant kernel's
+             event-timed duration, against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle on this host's cores over the same batch
+
+Under torchrun (N > 1) every rank searches its own replica of the index
+(weak scaling; the path needs no data exchange between replicas) and the
+slowest rank's time counts.
+"""
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "queries/s and % HBM roofline at exact top-k; p50/p99 latency served vs plain"
+WORKLOAD = ("config1 LSH-style index: 1,000,000 objects x 240 dims, uint32 bucket ids uniform in "
+            "[0,8192); 1,024 queries x 240 exact-match items (half derived from stored objects, 60% "
+            "of items redrawn); k=100; exact top-k ids+counts")
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--objects", type=int, default=1_000_000)
+    p.add_argument("--queries", type=int, default=1024)
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--no-autotune", action="store_true")
+    return p.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """traffic_bytes_per_launch recorded in profiles/ for this kernel/workload."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for name in sorted(os.listdir(pdir)):
+        if not name.endswith((".md", ".txt")):
+            continue
+        with open(os.path.join(pdir, name)) as f:
+            txt = f.read()
+        if "workload: config1" not in txt or ("kernel: " + kernel) not in txt:
+            continue
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+        if m:
+            return float(m.group(1))
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local, dist
+
+
+def max_over_ranks(x, dist, device_is_cuda):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if device_is_cuda else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_reference(args, world, rank):
+    """The reference's own CPU implementation of the path is its CPU
+    match-count oracle (test/test_compression_query.cu:127-284); here the
+    oracle restatement runs on all host threads over bounded samples."""
+    if rank != 0:
+        return
+    from genie_gb300 import workloads
+    from oracle import oracle
+    values, batch = workloads.config1(n=args.objects, q=args.queries)
+    ox = oracle.Index(values)
+    cores = os.cpu_count() or 1
+    sample_q = min(256, args.queries)
+    sub = dict(item_off=batch["item_off"][:sample_q + 1], dim=batch["dim"], low=batch["low"], up=batch["up"],
+               k=batch["k"][:sample_q])
+    for _ in range(max(1, args.warmup)):
+        ox.search(sub, n_threads=cores)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ox.search(sub, n_threads=cores)
+    dt = time.perf_counter() - t0
+    qps = sample_q * args.steps / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "step": "%d-query sample of the batch" % sample_q},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port",
+                         "sample": "%d queries of the config1 batch per step, %d steps" % (sample_q, args.steps)},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    world, rank, local, dist = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    import torch
+    import genie_gb300 as g
+    from genie_gb300 import build, workloads
+    build.build()
+    torch.cuda.set_device(local)
+    g._check(g.lib().genie_init(local))
+
+    values, batch = workloads.config1(n=args.objects, q=args.queries)
+    table = g.Table.from_values(values)
+    qb = g.QueryBatch(batch["item_off"], batch["dim"], batch["low"], batch["up"], batch["k"])
+    lay = table.layout()
+    alg_bytes = workloads.algorithmic_bytes(lay["key_offsets"], lay["key_base"], lay["dim_min"], lay["dim_max"],
+                                            batch)
+    n_items = int(batch["item_off"][-1])
+    Q = qb.n_queries
+
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")     # > 2x the 129 MB L2
+
+    bt = g.Batch(table, Q, n_items, 100, use_graph=True)
+    tuning = bt.tuning() if args.no_autotune else bt.autotune(qb)
+    bt.stage(qb)
+
+    # ---- value: device-resident batch, graph launches, L2 flushed per step
+    for _ in range(args.warmup):
+        flush.zero_()
+        bt.launch(stream.cuda_stream)
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for s, e in evs:
+        flush.zero_()
+        s.record(stream)
+        bt.launch(stream.cuda_stream)
+        e.record(stream)
+    torch.cuda.synchronize()
+    step_ms = [s.elapsed_time(e) for s, e in evs]
+    clock_info = clocks.stop()
+    total_ms = max_over_ranks(sum(step_ms), dist, True)
+    value = world * Q * args.steps / (total_ms / 1e3)
+    ids_graph, cnt_graph = bt.fetch()
+
+    # ---- roofline: per-kernel events (direct launches, same tuning and flushing)
+    bp = g.Batch(table, Q, n_items, 100, use_graph=False)
+    bp.set_tuning(**{k: v for k, v in tuning.items()})
+    bp.stage(qb)
+    stage_tot = np.zeros(5)
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        bp.launch(stream.cuda_stream)
+        ms = bp.stage_ms()
+        if i >= args.warmup:
+            stage_tot += ms
+    names = ["k_plan", "k_sparse<packed>", "k_sparse<wide>", "k_dense<u8>", "k_dense<u32>"]
+    dom = int(np.argmax(stage_tot[1:]) + 1)
+    dom_ms = stage_tot[dom] / args.steps
+    peak, peak_kind = peaks()
+    achieved = alg_bytes / (dom_ms / 1e3) / 1e9
+    traffic = ncu_traffic(names[dom])
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": names[dom], "kernel_ms": dom_ms,
+                "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind,
+                "stage_ms": {n: float(v / args.steps) for n, v in zip(names, stage_tot)}}
+
+    # ---- e2e through the public API from host buffers
+    for _ in range(max(1, args.warmup // 2)):
+        bt.run(qb)
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bt.run(qb)
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = max_over_ranks(sum(e2e_times), dist, True)
+    e2e = world * Q * args.steps / e2e_s
+    h2d = (Q + 1) * 8 * 2 + n_items * 12 + Q + Q * 4 + 8
+    d2h = qb.total_k * 8 + 4
+
+    # ---- plain per-batch path (genie_search) for the batched/plain ratio
+    for _ in range(max(1, args.warmup // 2)):
+        g.search(table, qb)
+    plain_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pid, pcnt = g.search(table, qb)
+        plain_times.append(time.perf_counter() - t0)
+    plain = world * Q * args.steps / max_over_ranks(sum(plain_times), dist, True)
+    same = bool(np.array_equal(pid, ids_graph) and np.array_equal(pcnt, cnt_graph))
+
+    # ---- CPU baseline: the oracle on this host's cores (rank 0)
+    cpu = None
+    if rank == 0:
+        from oracle import oracle
+        cores = os.cpu_count() or 1
+        t_build = time.perf_counter()
+        ox = oracle.Index(values)
+        t_build = time.perf_counter() - t_build
+        reps, t_cpu = 0, 0.0
+        while reps < 1 or t_cpu < args.cpu_seconds:
+            t0 = time.perf_counter()
+            oid, ocnt, _, _ = ox.search(qb.as_oracle_batch(), n_threads=cores)
+            t_cpu += time.perf_counter() - t0
+            reps += 1
+        cpu = {"value": Q * reps / t_cpu, "unit": "queries/s", "cores": cores, "kind": "port",
+               "sample": "the full %d-query batch x %d repetitions (oracle index build %.1f s, untimed)"
+                         % (Q, reps, t_build),
+               "matches_gpu": bool(np.array_equal(oid, ids_graph) and np.array_equal(ocnt, cnt_graph))}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded generator with the config1 shapes and distributions)",
+            "config": {"workload": WORKLOAD, "n_objects": args.objects, "n_dims": 240, "n_queries": Q, "k": 100,
+                       "l2": "flushed by a 512 MiB device write before every timed step",
+                       "tuning": tuning, "parallelism": "replica per GPU" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "plain_e2e": {"value": plain, "unit": "queries/s", "path": "genie_search (per-call upload, 5 launches)",
+                          "batched_over_plain": e2e / plain, "same_results": same},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clock_info,
+            "gpu_launches": 5 * args.steps,
+        }
+        print(json.dumps(line))
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

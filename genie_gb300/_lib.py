@@ -30,7 +30,7 @@ class GenieBatchConfig(ctypes.Structure):
 
 
 class GenieTuning(ctypes.Structure):
-    _fields_ = [("sparse_parts_cap", I32), ("sparse_threads", I32), ("dense_tile", I32),
+    _fields_ = [("sparse_slots", I32), ("sparse_ctas_per_sm", I32), ("dense_tile", I32),
                 ("dense_threads", I32), ("sparse_max_total", I64), ("dense_part_work", I64)]
 
 
@@ -52,14 +52,17 @@ PROTOTYPES = {
     "genie_index_load": (ctypes.c_int, [ctypes.c_char_p, P]),
     "genie_search": (ctypes.c_int, [P, P, P, P, P]),
     "genie_search_multi": (ctypes.c_int, [P, P, I32, P, P, P]),
-    "genie_search_device": (ctypes.c_int, [P, P, P, P, P, P, P]),
     "genie_batch_create": (ctypes.c_int, [P, P, P]),
     "genie_batch_destroy": (ctypes.c_int, [P]),
     "genie_batch_run": (ctypes.c_int, [P, P, P, P, P]),
+    "genie_batch_stage": (ctypes.c_int, [P, P]),
+    "genie_batch_launch": (ctypes.c_int, [P, P]),
+    "genie_batch_fetch": (ctypes.c_int, [P, P, P, P]),
     "genie_batch_autotune": (ctypes.c_int, [P, P, P]),
     "genie_batch_get_tuning": (ctypes.c_int, [P, P]),
     "genie_batch_set_tuning": (ctypes.c_int, [P, P]),
     "genie_batch_last_stats": (ctypes.c_int, [P, P, P]),
+    "genie_batch_stage_ms": (ctypes.c_int, [P, P]),
     "genie_codec_encode": (I64, [I32, P, I64, P, I64]),
     "genie_codec_encode_bound": (I64, [I64]),
     "genie_codec_decode_device": (ctypes.c_int, [I32, P, P, I64, P, P, P, P]),

@@ -1,5 +1,6 @@
 """Batched search handle (genie_batch_*): fixed-capacity device buffers,
-device-side query compile, persistent kernels in one CUDA graph."""
+pinned staging, device-side query compile, persistent kernels in one CUDA
+graph, and the autotuner."""
 import ctypes
 
 import numpy as np
@@ -8,34 +9,71 @@ from . import _lib
 
 
 class Batch:
-    def __init__(self, table, max_queries, max_items, max_k, use_graph=True, autotune=False):
+    def __init__(self, table, max_queries, max_items, max_k, use_graph=True):
         from . import _check, lib
-        cfg = _lib.GenieBatchConfig(int(max_queries), int(max_items), int(max_k), int(bool(use_graph)),
-                                    int(bool(autotune)))
+        cfg = _lib.GenieBatchConfig(int(max_queries), int(max_items), int(max_k), int(bool(use_graph)), 0)
         h = ctypes.c_void_p()
         _check(lib().genie_batch_create(table.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
         self.table = table
+        self._staged = None
 
-    def run(self, batch, scores=False):
-        from . import _check, lib
-        n = batch.total_k
+    def _outs(self, n, scores):
         ids = np.zeros(max(1, n), np.uint32)
         cnt = np.zeros(max(1, n), np.uint32)
         sc = np.zeros(max(1, n), np.float32) if scores else None
+        return ids, cnt, sc
+
+    def run(self, batch, scores=False):
+        """stage + launch + fetch (synchronous)."""
+        from . import _check, lib
+        n = batch.total_k
+        ids, cnt, sc = self._outs(n, scores)
         s = batch.struct()
         _check(lib().genie_batch_run(self._h, ctypes.byref(s), ids.ctypes.data, cnt.ctypes.data,
                                      None if sc is None else sc.ctypes.data))
-        if scores:
-            return ids[:n], cnt[:n], sc[:n]
-        return ids[:n], cnt[:n]
+        self._staged = batch
+        return (ids[:n], cnt[:n], sc[:n]) if scores else (ids[:n], cnt[:n])
+
+    def stage(self, batch):
+        from . import _check, lib
+        s = batch.struct()
+        _check(lib().genie_batch_stage(self._h, ctypes.byref(s)))
+        self._staged = batch
+
+    def launch(self, stream=None):
+        """Enqueue the device work of the staged batch on a cudaStream_t (int)."""
+        from . import _check, lib
+        _check(lib().genie_batch_launch(self._h, None if stream is None else ctypes.c_void_p(stream)))
+
+    def fetch(self, scores=False):
+        from . import _check, lib
+        n = self._staged.total_k
+        ids, cnt, sc = self._outs(n, scores)
+        _check(lib().genie_batch_fetch(self._h, ids.ctypes.data, cnt.ctypes.data,
+                                       None if sc is None else sc.ctypes.data))
+        return (ids[:n], cnt[:n], sc[:n]) if scores else (ids[:n], cnt[:n])
 
     def autotune(self, sample):
         from . import _check, lib
         t = _lib.GenieTuning()
         s = sample.struct()
         _check(lib().genie_batch_autotune(self._h, ctypes.byref(s), ctypes.byref(t)))
+        self._staged = sample
         return {f: getattr(t, f) for f, _ in _lib.GenieTuning._fields_}
+
+    def tuning(self):
+        from . import _check, lib
+        t = _lib.GenieTuning()
+        _check(lib().genie_batch_get_tuning(self._h, ctypes.byref(t)))
+        return {f: getattr(t, f) for f, _ in _lib.GenieTuning._fields_}
+
+    def set_tuning(self, **kw):
+        from . import _check, lib
+        t = _lib.GenieTuning()
+        for k, v in kw.items():
+            setattr(t, k, v)
+        _check(lib().genie_batch_set_tuning(self._h, ctypes.byref(t)))
 
     def last_stats(self):
         from . import _check, lib
@@ -43,6 +81,14 @@ class Batch:
         ms = ctypes.c_float()
         _check(lib().genie_batch_last_stats(self._h, ctypes.byref(k), ctypes.byref(ms)))
         return k.value, ms.value
+
+    def stage_ms(self):
+        """Per-stage device ms of the last launch (batches made with use_graph=False):
+        plan, sparse-packed, sparse-wide, dense-small, dense-wide."""
+        from . import _check, lib
+        ms = np.zeros(5, np.float32)
+        _check(lib().genie_batch_stage_ms(self._h, ms.ctypes.data))
+        return ms
 
     def close(self):
         from . import lib

@@ -1,0 +1,388 @@
+// batch.cu -- batched search: fixed-capacity buffers, pinned staging, the
+// device work of a batch captured once as a CUDA graph, and the autotuner.
+//
+// The reference runs one synchronous pipeline per batch: host query compile,
+// H2D of the compiled spans, match_AT, a host-synchronising overflow check,
+// heap_count_topk with cudaMalloc/cudaFree, D2H (matching/knn.cu:106-183,
+// match.cu:224-464).  Here the batch size lives in device memory, so the same
+// graph (memset + plan + four persistent kernels) serves every batch.
+#include "capi_internal.h"
+
+#include <cstring>
+#include <vector>
+
+using namespace gg;
+
+struct genie_batch {
+    genie_index *ix = nullptr;
+    genie_batch_config cfg{};
+    Workspace ws;
+    DevBuf dyn;
+    Tuning tuning{};
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    bool graph_valid = false;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t stage_ev[kStages + 1] = {};
+    // pinned staging
+    int64_t *h_item_off = nullptr, *h_out_off = nullptr;
+    int32_t *h_dim = nullptr, *h_low = nullptr, *h_up = nullptr;
+    float *h_weight = nullptr, *h_scores = nullptr;
+    uint8_t *h_weighted = nullptr;
+    uint32_t *h_k = nullptr, *h_dyn = nullptr, *h_ids = nullptr, *h_counts = nullptr, *h_err = nullptr;
+    int32_t staged_q = 0;
+    int64_t staged_sumk = 0;
+    int last_kernels = 0;
+    bool launched = false;
+    ~genie_batch();
+};
+
+genie_batch::~genie_batch() {
+    if (ix) cudaSetDevice(ix->device);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    for (cudaEvent_t e : stage_ev)
+        if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+    void *pinned[] = {h_item_off, h_out_off, h_dim, h_low, h_up, h_weight, h_scores, h_weighted, h_k, h_dyn,
+                      h_ids, h_counts, h_err};
+    for (void *p : pinned)
+        if (p) cudaFreeHost(p);
+    ws.release();
+    dyn.release();
+}
+
+namespace {
+
+template <class T>
+cudaError_t pin(T *&p, size_t n) {
+    return cudaMallocHost((void **)&p, n * sizeof(T) + 64);
+}
+
+DevQueries device_queries(const genie_batch *b) {
+    DevQueries q;
+    q.n_queries = b->cfg.max_queries;
+    q.item_off = (const int64_t *)b->ws.item_off.p;
+    q.dim = (const int32_t *)b->ws.dim.p;
+    q.low = (const int32_t *)b->ws.low.p;
+    q.up = (const int32_t *)b->ws.up.p;
+    q.weight = (const float *)b->ws.weight.p;
+    q.weighted = (const uint8_t *)b->ws.weighted.p;
+    q.k = (const uint32_t *)b->ws.k.p;
+    q.uniform_k = 0;
+    q.out_off = (const int64_t *)b->ws.out_off.p;
+    q.dyn = (const uint32_t *)b->dyn.p;
+    return q;
+}
+
+int enqueue(genie_batch *b, cudaStream_t s) {
+    DeviceContext &ctx = device_context(b->ix->device);
+    const DevQueries q = device_queries(b);
+    const Work w = b->ws.view(b->cfg.max_queries, true);
+    if (!b->cfg.use_graph) {
+        // direct launches, with an event after every stage for per-kernel timing
+        b->last_kernels = launch_match(b->ix->dev, q, w, b->tuning, ctx.num_sms, s, b->stage_ev);
+        cudaError_t e = cudaGetLastError();
+        return e ? cuda_fail(e, "batch launch") : GENIE_OK;
+    }
+    if (!b->graph_valid) {
+        if (b->gexec) cudaGraphExecDestroy(b->gexec);
+        b->gexec = nullptr;
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+        if (e) return cuda_fail(e, "graph capture");
+        b->last_kernels = launch_match(b->ix->dev, q, w, b->tuning, ctx.num_sms, b->stream);
+        cudaError_t le = cudaGetLastError();
+        e = cudaStreamEndCapture(b->stream, &g);
+        if (le) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(le, "graph capture launch");
+        }
+        if (e) return cuda_fail(e, "graph capture end");
+        e = cudaGraphInstantiate(&b->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e) return cuda_fail(e, "graph instantiate");
+        b->graph_valid = true;
+    }
+    cudaError_t e = cudaGraphLaunch(b->gexec, s);
+    return e ? cuda_fail(e, "graph launch") : GENIE_OK;
+}
+
+// Validate and copy a batch into pinned staging, then to the device (async on s).
+int stage_async(genie_batch *b, const genie_queries *q, cudaStream_t s) {
+    std::vector<int64_t> out_off;
+    int64_t n_items = 0;
+    int rc = validate_queries(q, out_off, n_items);
+    if (rc) return rc;
+    const int64_t Q = q->n_queries;
+    if (Q > b->cfg.max_queries) return fail(GENIE_ERR_INVALID_ARG, "%lld queries exceed the batch capacity %d", (long long)Q, b->cfg.max_queries);
+    if (n_items > b->cfg.max_items) return fail(GENIE_ERR_INVALID_ARG, "%lld items exceed the batch capacity %lld", (long long)n_items, (long long)b->cfg.max_items);
+    for (int64_t i = 0; i < Q; ++i) {
+        const uint32_t k = q->k ? q->k[i] : q->uniform_k;
+        if (k > b->cfg.max_k) return fail(GENIE_ERR_INVALID_ARG, "k=%u exceeds the batch capacity %u", k, b->cfg.max_k);
+    }
+    memcpy(b->h_item_off, q->item_off, (Q + 1) * 8);
+    memcpy(b->h_dim, q->dim, n_items * 4);
+    memcpy(b->h_low, q->low, n_items * 4);
+    memcpy(b->h_up, q->up, n_items * 4);
+    if (q->weighted && q->weight) {
+        memcpy(b->h_weight, q->weight, n_items * 4);
+        memcpy(b->h_weighted, q->weighted, Q);
+    } else {
+        memset(b->h_weighted, 0, Q);
+    }
+    for (int64_t i = 0; i < Q; ++i) b->h_k[i] = q->k ? q->k[i] : q->uniform_k;
+    memcpy(b->h_out_off, out_off.data(), (Q + 1) * 8);
+    b->h_dyn[0] = (uint32_t)Q;
+    b->h_dyn[1] = q->uniform_k;
+    cudaError_t e = cudaSuccess;
+    Workspace &ws = b->ws;
+    auto h2d = [&](void *dst, const void *src, size_t n) {
+        if (n && !e) e = cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s);
+    };
+    h2d(ws.item_off.p, b->h_item_off, (Q + 1) * 8);
+    h2d(ws.dim.p, b->h_dim, n_items * 4);
+    h2d(ws.low.p, b->h_low, n_items * 4);
+    h2d(ws.up.p, b->h_up, n_items * 4);
+    if (q->weighted && q->weight) h2d(ws.weight.p, b->h_weight, n_items * 4);
+    h2d(ws.weighted.p, b->h_weighted, Q);
+    h2d(ws.k.p, b->h_k, Q * 4);
+    h2d(ws.out_off.p, b->h_out_off, (Q + 1) * 8);
+    h2d(b->dyn.p, b->h_dyn, 8);
+    if (e) return cuda_fail(e, "batch upload");
+    b->staged_q = (int32_t)Q;
+    b->staged_sumk = out_off[Q];
+    return GENIE_OK;
+}
+
+int fetch_async(genie_batch *b, cudaStream_t s, bool scores) {
+    const int64_t n = b->staged_sumk;
+    const Work w = b->ws.view(b->cfg.max_queries, true);
+    cudaError_t e = cudaMemcpyAsync(b->h_err, w.ctr + kCtrError, 4, cudaMemcpyDeviceToHost, s);
+    if (!e && n) e = cudaMemcpyAsync(b->h_ids, w.out_ids, n * 4, cudaMemcpyDeviceToHost, s);
+    if (!e && n) e = cudaMemcpyAsync(b->h_counts, w.out_counts, n * 4, cudaMemcpyDeviceToHost, s);
+    if (!e && n && scores) e = cudaMemcpyAsync(b->h_scores, w.out_scores, n * 4, cudaMemcpyDeviceToHost, s);
+    return e ? cuda_fail(e, "batch download") : GENIE_OK;
+}
+
+int finish_fetch(genie_batch *b, uint32_t *ids, uint32_t *counts, float *scores) {
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e) return cuda_fail(e, "batch");
+    int rc = check_device_error(*b->h_err);
+    if (rc) return rc;
+    const size_t n = (size_t)b->staged_sumk;
+    if (ids) memcpy(ids, b->h_ids, n * 4);
+    if (counts) memcpy(counts, b->h_counts, n * 4);
+    if (scores) memcpy(scores, b->h_scores, n * 4);
+    return GENIE_OK;
+}
+
+Tuning from_public(const Tuning &base, const genie_tuning &t) {
+    Tuning r = base;
+    if (t.sparse_slots > 0) {
+        r.sparse_slots_packed = (t.sparse_slots + 31) & ~31;
+        r.sparse_slots_wide = ((t.sparse_slots / 2) + 31) & ~31;
+    }
+    if (t.sparse_ctas_per_sm > 0) r.sparse_ctas_per_sm = t.sparse_ctas_per_sm;
+    if (t.dense_tile > 0) {
+        r.dense_tile_u8 = (t.dense_tile + 255) & ~255;
+        r.dense_tile_u32 = ((t.dense_tile / 4) + 63) & ~63;
+    }
+    if (t.dense_threads > 0) r.dense_threads = t.dense_threads;
+    if (t.sparse_max_total > 0) r.sparse_max_total = t.sparse_max_total;
+    if (t.dense_part_work > 0) r.dense_part_work = t.dense_part_work;
+    return r;
+}
+
+void to_public(const Tuning &r, genie_tuning &t) {
+    t.sparse_slots = r.sparse_slots_packed;
+    t.sparse_ctas_per_sm = r.sparse_ctas_per_sm;
+    t.dense_tile = r.dense_tile_u8;
+    t.dense_threads = r.dense_threads;
+    t.sparse_max_total = r.sparse_max_total;
+    t.dense_part_work = r.dense_part_work;
+}
+
+}  // namespace
+
+extern "C" {
+
+int genie_batch_create(genie_index *ix, const genie_batch_config *cfg, genie_batch **out) {
+    if (!ix || !cfg || !out) return fail(GENIE_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    if (cfg->max_queries <= 0 || cfg->max_items < 0 || cfg->max_k == 0 || cfg->max_k > (uint32_t)kMaxK)
+        return fail(GENIE_ERR_INVALID_ARG, "batch capacity must hold >= 1 query and 1 <= max_k <= %d", kMaxK);
+    cudaSetDevice(ix->device);
+    genie_batch *b = new genie_batch();
+    b->ix = ix;
+    b->cfg = *cfg;
+    b->tuning = ix->tuning;
+    const int64_t Q = cfg->max_queries, I = cfg->max_items > 0 ? cfg->max_items : 1, K = (int64_t)Q * cfg->max_k;
+    cudaError_t e = b->ws.reserve(Q, I, K);
+    if (!e) e = b->dyn.reserve(16);
+    if (!e) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (!e) e = cudaEventCreate(&b->ev0);
+    if (!e) e = cudaEventCreate(&b->ev1);
+    for (int i = 0; i <= kStages && !e; ++i) e = cudaEventCreate(&b->stage_ev[i]);
+    if (!e) e = pin(b->h_item_off, Q + 1);
+    if (!e) e = pin(b->h_out_off, Q + 1);
+    if (!e) e = pin(b->h_dim, I);
+    if (!e) e = pin(b->h_low, I);
+    if (!e) e = pin(b->h_up, I);
+    if (!e) e = pin(b->h_weight, I);
+    if (!e) e = pin(b->h_weighted, Q);
+    if (!e) e = pin(b->h_k, Q);
+    if (!e) e = pin(b->h_dyn, 4);
+    if (!e) e = pin(b->h_ids, K);
+    if (!e) e = pin(b->h_counts, K);
+    if (!e) e = pin(b->h_scores, K);
+    if (!e) e = pin(b->h_err, 4);
+    if (e) {
+        delete b;
+        return cuda_fail(e, "batch buffers");
+    }
+    *out = b;
+    return GENIE_OK;
+}
+
+int genie_batch_destroy(genie_batch *b) {
+    delete b;
+    return GENIE_OK;
+}
+
+int genie_batch_stage(genie_batch *b, const genie_queries *q) {
+    if (!b) return fail(GENIE_ERR_INVALID_ARG, "batch is NULL");
+    cudaSetDevice(b->ix->device);
+    int rc = stage_async(b, q, b->stream);
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    return e ? cuda_fail(e, "batch upload") : GENIE_OK;
+}
+
+int genie_batch_launch(genie_batch *b, void *stream) {
+    if (!b) return fail(GENIE_ERR_INVALID_ARG, "batch is NULL");
+    cudaSetDevice(b->ix->device);
+    cudaStream_t s = stream ? (cudaStream_t)stream : b->stream;
+    cudaEventRecord(b->ev0, s);
+    int rc = enqueue(b, s);
+    cudaEventRecord(b->ev1, s);
+    b->launched = rc == GENIE_OK;
+    return rc;
+}
+
+int genie_batch_fetch(genie_batch *b, uint32_t *out_ids, uint32_t *out_counts, float *out_scores) {
+    if (!b) return fail(GENIE_ERR_INVALID_ARG, "batch is NULL");
+    cudaSetDevice(b->ix->device);
+    cudaStreamWaitEvent(b->stream, b->ev1, 0);
+    int rc = fetch_async(b, b->stream, out_scores != nullptr);
+    if (rc) return rc;
+    return finish_fetch(b, out_ids, out_counts, out_scores);
+}
+
+int genie_batch_run(genie_batch *b, const genie_queries *q, uint32_t *out_ids, uint32_t *out_counts,
+                    float *out_scores) {
+    if (!b) return fail(GENIE_ERR_INVALID_ARG, "batch is NULL");
+    cudaSetDevice(b->ix->device);
+    int rc = stage_async(b, q, b->stream);
+    if (rc) return rc;
+    if (b->staged_q == 0) return GENIE_OK;
+    cudaEventRecord(b->ev0, b->stream);
+    rc = enqueue(b, b->stream);
+    cudaEventRecord(b->ev1, b->stream);
+    if (rc) return rc;
+    rc = fetch_async(b, b->stream, out_scores != nullptr);
+    if (rc) return rc;
+    return finish_fetch(b, out_ids, out_counts, out_scores);
+}
+
+int genie_batch_get_tuning(const genie_batch *b, genie_tuning *out) {
+    if (!b || !out) return fail(GENIE_ERR_INVALID_ARG, "NULL argument");
+    to_public(b->tuning, *out);
+    return GENIE_OK;
+}
+
+int genie_batch_set_tuning(genie_batch *b, const genie_tuning *t) {
+    if (!b || !t) return fail(GENIE_ERR_INVALID_ARG, "NULL argument");
+    Tuning r = from_public(b->tuning, *t);
+    if (r.sparse_slots_packed < 1024 || sparse_smem_bytes(r, true) > 227 * 1024 ||
+        sparse_smem_bytes(r, false) > 227 * 1024 || r.dense_tile_u8 < 4096 ||
+        dense_smem_bytes(r, true) > 227 * 1024 || dense_smem_bytes(r, false) > 227 * 1024 ||
+        (r.dense_threads != 512 && r.dense_threads != 1024))
+        return fail(GENIE_ERR_INVALID_ARG, "tuning outside the supported shapes");
+    b->tuning = r;
+    b->graph_valid = false;
+    return GENIE_OK;
+}
+
+int genie_batch_last_stats(const genie_batch *b, int32_t *kernels, float *device_ms) {
+    if (!b) return fail(GENIE_ERR_INVALID_ARG, "batch is NULL");
+    if (kernels) *kernels = b->last_kernels;
+    if (device_ms) {
+        *device_ms = 0.0f;
+        if (b->launched) {
+            cudaEventSynchronize(b->ev1);
+            cudaEventElapsedTime(device_ms, b->ev0, b->ev1);
+        }
+    }
+    return GENIE_OK;
+}
+
+int genie_batch_stage_ms(const genie_batch *b, float *ms) {
+    if (!b || !ms) return fail(GENIE_ERR_INVALID_ARG, "NULL argument");
+    if (b->cfg.use_graph) return fail(GENIE_ERR_INVALID_ARG, "per-kernel times need a batch created with use_graph = 0");
+    if (!b->launched) return fail(GENIE_ERR_INVALID_ARG, "no launch yet");
+    cudaEventSynchronize(b->stage_ev[kStages]);
+    for (int i = 0; i < kStages; ++i) {
+        ms[i] = 0.0f;
+        cudaEventElapsedTime(&ms[i], b->stage_ev[i], b->stage_ev[i + 1]);
+    }
+    return GENIE_OK;
+}
+
+// Times each candidate shape on the sample (one warm-up, three timed graph
+// launches) and keeps the fastest.  Candidates vary the hash slots per CTA
+// (hence CTAs per SM), the dense tile and the sparse/dense crossover.
+int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuning *chosen) {
+    if (!b || !sample) return fail(GENIE_ERR_INVALID_ARG, "NULL argument");
+    cudaSetDevice(b->ix->device);
+    int rc = genie_batch_stage(b, sample);
+    if (rc) return rc;
+    const Tuning base = b->tuning;
+    struct Cand { int32_t slots, tile; int64_t smax; };
+    const Cand cands[] = {
+        {22528, 147456, 16 * 16896}, {11264, 147456, 16 * 16896}, {33792, 147456, 16 * 16896},
+        {22528, 98304, 16 * 16896}, {22528, 196608, 16 * 16896}, {22528, 147456, 4 * 16896},
+        {22528, 147456, 64 * 16896},
+    };
+    float best_ms = 1e30f;
+    Tuning best = base;
+    for (const Cand &c : cands) {
+        genie_tuning t{};
+        t.sparse_slots = c.slots;
+        t.dense_tile = c.tile;
+        t.sparse_max_total = c.smax;
+        if (genie_batch_set_tuning(b, &t)) continue;
+        float total = 0.0f;
+        bool ok = true;
+        for (int it = 0; it < 4 && ok; ++it) {
+            if (genie_batch_launch(b, nullptr)) { ok = false; break; }
+            float ms = 0.0f;
+            genie_batch_last_stats(b, nullptr, &ms);
+            if (it > 0) total += ms;
+        }
+        cudaError_t e = cudaStreamSynchronize(b->stream);
+        if (e) return cuda_fail(e, "autotune");
+        if (ok && total < best_ms) {
+            best_ms = total;
+            best = b->tuning;
+        }
+        b->tuning = base;
+    }
+    b->tuning = best;
+    b->graph_valid = false;
+    if (chosen) to_public(best, *chosen);
+    return GENIE_OK;
+}
+
+}  // extern "C"

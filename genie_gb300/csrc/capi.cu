@@ -56,7 +56,7 @@ DeviceContext &device_context(int dev) {
     if (!c.ready) {
         cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, dev);
         c.tuning = default_tuning();
-        prepare_kernels_max();
+        c.prepare_error = prepare_kernels_max();
         c.ready = true;
     }
     return c;
@@ -256,6 +256,7 @@ int run_search(genie_index *ix, const genie_queries *q, const std::vector<int64_
     dq.k = q->k ? (const uint32_t *)ws.k.p : nullptr;
     dq.uniform_k = q->uniform_k;
     dq.out_off = (const int64_t *)ws.out_off.p;
+    dq.dyn = nullptr;
     Work w = ws.view(Q, out_scores != nullptr);
     DeviceContext &ctx = device_context(ix->device);
     ix->last_launches = launch_match(ix->dev, dq, w, ix->tuning, ctx.num_sms, s);
@@ -302,6 +303,7 @@ int genie_init(int device) {
 static genie_index *new_index() {
     int dev = 0;
     cudaGetDevice(&dev);
+    if (device_context(dev).prepare_error != cudaSuccess) return nullptr;
     genie_index *ix = new genie_index();
     ix->device = dev;
     ix->tuning = device_context(dev).tuning;
@@ -314,6 +316,7 @@ int genie_index_create(const int32_t *values, int64_t n_objects, int32_t n_dims,
     *out = nullptr;
     if (!values || n_objects <= 0 || n_dims <= 0) return fail(GENIE_ERR_INVALID_ARG, "no data input");
     genie_index *ix = new_index();
+    if (!ix) return cuda_fail(device_context(0).prepare_error, "kernel setup");
     if (!build_host_index(values, n_objects, n_dims, ix->host)) {
         delete ix;
         return fail(GENIE_ERR_INVALID_ARG, "index build failed (N must be < 2^32)");
@@ -326,6 +329,7 @@ int genie_index_create_bag(const int32_t *values, const int64_t *row_off, int64_
     *out = nullptr;
     if (!values || !row_off || n_objects <= 0) return fail(GENIE_ERR_INVALID_ARG, "no data input");
     genie_index *ix = new_index();
+    if (!ix) return cuda_fail(device_context(0).prepare_error, "kernel setup");
     if (!build_host_index_bag(values, row_off, n_objects, ix->host)) {
         delete ix;
         return fail(GENIE_ERR_INVALID_ARG, "bag index build failed");
@@ -430,12 +434,6 @@ int genie_search_multi(genie_index *const *ixs, const genie_queries *qs, int32_t
         ixs[i]->mu.unlock();
     }
     return rc;
-}
-
-int genie_search_device(genie_index *ix, const genie_queries *q, const int64_t *out_off_dev, uint32_t *out_ids,
-                        uint32_t *out_counts, float *out_scores, void *stream) {
-    (void)ix; (void)q; (void)out_off_dev; (void)out_ids; (void)out_counts; (void)out_scores; (void)stream;
-    return fail(GENIE_ERR_NOT_IMPLEMENTED, "use genie_batch_* for device-resident query batches");
 }
 
 }  // extern "C"

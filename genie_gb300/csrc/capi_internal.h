@@ -28,6 +28,7 @@ struct DevBuf {
 struct DeviceContext {
     bool ready = false;
     int num_sms = 0;
+    cudaError_t prepare_error = cudaSuccess;
     Tuning tuning;
 };
 DeviceContext &device_context(int dev);

@@ -56,6 +56,9 @@ struct DevQueries {
     const uint32_t *k;
     uint32_t uniform_k;
     const int64_t *out_off;
+    // optional device-side size of a captured batch: dyn[0] = queries in this
+    // run (<= n_queries, the capacity), dyn[1] = uniform k
+    const uint32_t *dyn;
 };
 
 // Per-query plan written by k_plan.

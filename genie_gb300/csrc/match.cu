@@ -22,11 +22,12 @@ namespace gg {
 // sparse/dense decision with the number of id-range parts.
 __global__ void __launch_bounds__(256) k_plan(DevIndex ix, DevQueries Q, Work W, Tuning T) {
     const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (q >= Q.n_queries) return;
+    const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
+    if (q >= nq) return;
     const uint32_t lane = lane_id();
     const int64_t i0 = Q.item_off[q], i1 = Q.item_off[q + 1];
     const int32_t m = (int32_t)(i1 - i0);
-    const uint32_t k = Q.k ? Q.k[q] : Q.uniform_k;
+    const uint32_t k = Q.k ? Q.k[q] : (Q.dyn ? Q.dyn[1] : Q.uniform_k);
     const bool weighted = Q.weighted && Q.weight && Q.weighted[q];
     int32_t scale = 0;
     if (weighted) {
@@ -624,28 +625,44 @@ cudaError_t prepare_kernels_max() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (optin <= 0) optin = 227 * 1024;
-    cudaError_t e;
-    if ((e = set_smem((const void *)k_sparse<true>, optin))) return e;
-    if ((e = set_smem((const void *)k_sparse<false>, optin))) return e;
-    if ((e = set_smem((const void *)k_dense<true>, optin))) return e;
-    if ((e = set_smem((const void *)k_dense<false>, optin))) return e;
+    const void *fns[] = {(const void *)k_sparse<true>, (const void *)k_sparse<false>,
+                         (const void *)k_dense<true>, (const void *)k_dense<false>};
+    for (const void *fn : fns) {
+        cudaFuncAttributes a;
+        cudaError_t e = cudaFuncGetAttributes(&a, fn);
+        if (e) return e;
+        // static and dynamic shared memory together may not exceed the opt-in limit
+        if ((e = set_smem(fn, (size_t)optin - a.sharedSizeBytes))) return e;
+    }
     return cudaSuccess;
 }
 
 int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t,
-                 int num_sms, cudaStream_t s) {
+                 int num_sms, cudaStream_t s, cudaEvent_t *ev) {
     if (Q.n_queries <= 0) return 0;
     int launches = 0;
+    if (ev) cudaEventRecord(ev[0], s);
     cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), s);
     const int plan_blocks = (int)((Q.n_queries * 32LL + 255) / 256);
     k_plan<<<plan_blocks, 256, 0, s>>>(ix, Q, W, t);
     ++launches;
-    const int sg = num_sms * std::max(1, t.sparse_ctas_per_sm);
-    k_sparse<true><<<sg, t.sparse_threads, sparse_smem_bytes(t, true), s>>>(ix, Q, W, t);
-    k_sparse<false><<<sg, t.sparse_threads, sparse_smem_bytes(t, false), s>>>(ix, Q, W, t);
-    const int dg = num_sms * std::max(1, t.dense_ctas_per_sm);
-    k_dense<true><<<dg, t.dense_threads, dense_smem_bytes(t, true), s>>>(ix, Q, W, t);
-    k_dense<false><<<dg, t.dense_threads, dense_smem_bytes(t, false), s>>>(ix, Q, W, t);
+    if (ev) cudaEventRecord(ev[1], s);
+    // persistent grids: as many CTAs as fit on every SM at once
+    auto grid = [&](const void *fn, int threads, size_t smem) {
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+        return num_sms * std::max(1, per_sm);
+    };
+    const size_t sp = sparse_smem_bytes(t, true), sw = sparse_smem_bytes(t, false);
+    const size_t dp = dense_smem_bytes(t, true), dw = dense_smem_bytes(t, false);
+    k_sparse<true><<<grid((const void *)k_sparse<true>, t.sparse_threads, sp), t.sparse_threads, sp, s>>>(ix, Q, W, t);
+    if (ev) cudaEventRecord(ev[2], s);
+    k_sparse<false><<<grid((const void *)k_sparse<false>, t.sparse_threads, sw), t.sparse_threads, sw, s>>>(ix, Q, W, t);
+    if (ev) cudaEventRecord(ev[3], s);
+    k_dense<true><<<grid((const void *)k_dense<true>, t.dense_threads, dp), t.dense_threads, dp, s>>>(ix, Q, W, t);
+    if (ev) cudaEventRecord(ev[4], s);
+    k_dense<false><<<grid((const void *)k_dense<false>, t.dense_threads, dw), t.dense_threads, dw, s>>>(ix, Q, W, t);
+    if (ev) cudaEventRecord(ev[5], s);
     launches += 4;
     return launches;
 }

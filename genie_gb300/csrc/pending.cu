@@ -18,26 +18,6 @@ int genie_index_create_compressed(const int32_t *, int64_t, int32_t, int32_t, in
 int genie_index_copy_compressed(const genie_index *, uint32_t *, int64_t *, int64_t *, uint32_t *, uint32_t *) {
     return fail(GENIE_ERR_NOT_IMPLEMENTED, "compressed indexes are not available in this build");
 }
-int genie_batch_create(genie_index *, const genie_batch_config *, genie_batch **out) {
-    if (out) *out = nullptr;
-    return fail(GENIE_ERR_NOT_IMPLEMENTED, "batched search is not available in this build");
-}
-int genie_batch_destroy(genie_batch *) { return GENIE_OK; }
-int genie_batch_run(genie_batch *, const genie_queries *, uint32_t *, uint32_t *, float *) {
-    return fail(GENIE_ERR_NOT_IMPLEMENTED, "batched search is not available in this build");
-}
-int genie_batch_autotune(genie_batch *, const genie_queries *, genie_tuning *) {
-    return fail(GENIE_ERR_NOT_IMPLEMENTED, "batched search is not available in this build");
-}
-int genie_batch_get_tuning(const genie_batch *, genie_tuning *) {
-    return fail(GENIE_ERR_NOT_IMPLEMENTED, "batched search is not available in this build");
-}
-int genie_batch_set_tuning(genie_batch *, const genie_tuning *) {
-    return fail(GENIE_ERR_NOT_IMPLEMENTED, "batched search is not available in this build");
-}
-int genie_batch_last_stats(const genie_batch *, int32_t *, float *) {
-    return fail(GENIE_ERR_NOT_IMPLEMENTED, "batched search is not available in this build");
-}
 int64_t genie_codec_encode(int32_t, const uint32_t *, int64_t, uint32_t *, int64_t) { return -GENIE_ERR_NOT_IMPLEMENTED; }
 int64_t genie_codec_encode_bound(int64_t n) { return (5 * n) / 4 + 96; }
 int genie_codec_decode_device(int32_t, const uint32_t *, const int64_t *, int64_t, const int64_t *, uint32_t *,

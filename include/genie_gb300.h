@@ -160,43 +160,55 @@ int genie_search(genie_index *ix, const genie_queries *q, uint32_t *out_ids,
 int genie_search_multi(genie_index *const *ix, const genie_queries *q, int32_t n_index,
                        uint32_t *out_ids, uint32_t *out_counts, float *out_scores);
 
-/* Search with every pointer in device memory on the given cudaStream_t
- * (NULL = the legacy default stream); asynchronous. */
-int genie_search_device(genie_index *ix, const genie_queries *q_dev, const int64_t *out_off_dev,
-                        uint32_t *out_ids, uint32_t *out_counts, float *out_scores,
-                        void *stream);
-
 /* ---------------------------------------------------------------- batched */
 
 typedef struct {
     int32_t max_queries;     /* capacity of one run */
     int64_t max_items;
     uint32_t max_k;
-    int32_t use_graph;       /* capture the run as one CUDA graph */
-    int32_t autotune;        /* pick tile/table sizes by timing candidates */
+    int32_t use_graph;       /* capture the device work as one CUDA graph */
+    int32_t autotune;        /* reserved: tune with genie_batch_autotune */
 } genie_batch_config;
 
+/* Kernel shape knobs picked by the autotuner (0 keeps the current value). */
 typedef struct {
-    int32_t sparse_parts_cap;   /* hash slots per CTA */
-    int32_t sparse_threads;
-    int32_t dense_tile;         /* ids per dense tile */
+    int32_t sparse_slots;       /* hash slots per CTA (4-byte slots; 8-byte get half) */
+    int32_t sparse_ctas_per_sm;
+    int32_t dense_tile;         /* ids per dense tile (1-byte counters; 4-byte get a quarter) */
     int32_t dense_threads;
-    int64_t sparse_max_total;   /* queries touching more ids go dense */
-    int64_t dense_part_work;    /* ids per dense part */
+    int64_t sparse_max_total;   /* queries touching more posting ids go dense */
+    int64_t dense_part_work;    /* posting ids per dense id-range part */
 } genie_tuning;
 
-/* Batched search: fixed-capacity device buffers, device-side query compile,
- * persistent match kernels, optional CUDA-graph capture and autotuning. */
+/* Batched search over one resident index: fixed-capacity device buffers,
+ * pinned host staging, the batch size read on the device, and the device
+ * work (query compile, persistent sparse/dense kernels, top-k, merge)
+ * captured once as a CUDA graph.  Beyond the reference, which supports one k
+ * per batch (knn.cu:158-159), every query carries its own k and weights. */
 int genie_batch_create(genie_index *ix, const genie_batch_config *cfg, genie_batch **out);
 int genie_batch_destroy(genie_batch *b);
+/* stage + launch + fetch, synchronous. */
 int genie_batch_run(genie_batch *b, const genie_queries *q, uint32_t *out_ids,
                     uint32_t *out_counts, float *out_scores);
-/* Tune on a sample batch (timing on the device), then keep the winner. */
+/* Validate a batch and copy it to the device (returns when it is resident). */
+int genie_batch_stage(genie_batch *b, const genie_queries *q);
+/* Enqueue the device work of the staged batch on `stream` (a cudaStream_t;
+ * NULL = the batch's own stream).  Asynchronous; may be repeated. */
+int genie_batch_launch(genie_batch *b, void *stream);
+/* Wait for the last launch and copy its results to host buffers. */
+int genie_batch_fetch(genie_batch *b, uint32_t *out_ids, uint32_t *out_counts, float *out_scores);
+/* Time candidate tunings on a sample batch on the device; keeps the fastest. */
 int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuning *chosen);
 int genie_batch_get_tuning(const genie_batch *b, genie_tuning *out);
 int genie_batch_set_tuning(genie_batch *b, const genie_tuning *t);
-/* Launch statistics of the last run: kernels launched, device milliseconds. */
+/* Statistics of the last launch: kernels launched, device milliseconds
+ * (between events around the device work; waits for it to finish). */
 int genie_batch_last_stats(const genie_batch *b, int32_t *kernels, float *device_ms);
+/* Device milliseconds of each stage of the last launch of a batch created
+ * with use_graph = 0: ms[0] plan (+ counter reset), ms[1] sparse 4-byte-slot
+ * kernel, ms[2] sparse 8-byte-slot kernel, ms[3] dense 1-byte-counter kernel,
+ * ms[4] dense 4-byte-counter kernel. */
+int genie_batch_stage_ms(const genie_batch *b, float *ms);
 
 /* ---------------------------------------------------------------- codecs */
 

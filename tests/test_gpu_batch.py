@@ -1,0 +1,85 @@
+"""Batched search (CUDA graph, device-side batch size, autotuner) against
+the oracle and the plain per-batch path."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _qb(genie, b):
+    return genie.QueryBatch(b["item_off"], b["dim"], b["low"], b["up"], b["k"], b.get("weight"), b.get("weighted"))
+
+
+def _slice(b, q0, q1):
+    off = b["item_off"]
+    a, z = off[q0], off[q1]
+    out = dict(item_off=off[q0:q1 + 1] - a, dim=b["dim"][a:z], low=b["low"][a:z], up=b["up"][a:z],
+               k=b["k"][q0:q1])
+    if b.get("weight") is not None:
+        out["weight"] = b["weight"][a:z]
+        out["weighted"] = b["weighted"][q0:q1]
+    return out
+
+
+def test_graph_batch_varying_sizes(genie, oracle):
+    from genie_gb300 import workloads
+    values, batch = workloads.config3(n=300_000, q=64)
+    t = genie.Table.from_values(values)
+    ox = oracle.Index(values)
+    bt = genie.Batch(t, max_queries=64, max_items=int(batch["item_off"][-1]), max_k=100)
+    for q0, q1 in ((0, 64), (5, 9), (10, 60), (0, 1)):
+        sub = _slice(batch, q0, q1)
+        qb = _qb(genie, sub)
+        ids, cnt, sc = bt.run(qb, scores=True)
+        oid, ocnt, osc, _ = ox.search(qb.as_oracle_batch())
+        assert np.array_equal(ids, oid) and np.array_equal(cnt, ocnt) and np.array_equal(sc, osc)
+        pid, pcnt = genie.search(t, qb)
+        assert np.array_equal(ids, pid) and np.array_equal(cnt, pcnt)
+    kernels, ms = bt.last_stats()
+    assert kernels >= 5 and ms > 0
+
+
+def test_stage_launch_fetch_repeatable(genie, oracle):
+    from genie_gb300 import workloads
+    values, batch = workloads.config1(n=100_000, q=64, k=100)
+    t = genie.Table.from_values(values)
+    qb = _qb(genie, batch)
+    bt = genie.Batch(t, 64, int(batch["item_off"][-1]), 100)
+    bt.stage(qb)
+    first = None
+    for _ in range(3):
+        bt.launch()
+        got = bt.fetch()
+        if first is None:
+            first = got
+        assert all(np.array_equal(a, b) for a, b in zip(got, first))
+    oid, ocnt, _, _ = oracle.Index(values).search(qb.as_oracle_batch())
+    assert np.array_equal(first[0], oid) and np.array_equal(first[1], ocnt)
+
+
+def test_autotune_keeps_results_exact(genie, oracle):
+    from genie_gb300 import workloads
+    values, batch = workloads.config3(n=200_000, q=32)
+    t = genie.Table.from_values(values)
+    qb = _qb(genie, batch)
+    bt = genie.Batch(t, 32, int(batch["item_off"][-1]), 100)
+    chosen = bt.autotune(qb)
+    assert chosen["sparse_slots"] > 0 and chosen["dense_tile"] > 0
+    ids, cnt = bt.run(qb)
+    oid, ocnt, _, _ = oracle.Index(values).search(qb.as_oracle_batch())
+    assert np.array_equal(ids, oid) and np.array_equal(cnt, ocnt)
+    # a smaller hash (more parts per query) and a smaller tile give the same answer
+    bt.set_tuning(sparse_slots=4096, dense_tile=16384)
+    ids2, cnt2 = bt.run(qb)
+    assert np.array_equal(ids2, oid) and np.array_equal(cnt2, ocnt)
+
+
+def test_batch_capacity_errors(genie):
+    t = genie.Table.from_values(np.zeros((10, 2), np.int32))
+    bt = genie.Batch(t, 2, 4, 5)
+    with pytest.raises(genie.cpu_runtime_error):
+        bt.run(genie.QueryBatch([0, 1, 2, 3], [0, 0, 0], [0, 0, 0], [0, 0, 0], 5))
+    with pytest.raises(genie.cpu_runtime_error):
+        bt.run(genie.QueryBatch([0, 1], [0], [0], [0], 6))
+    ids, cnt = bt.run(genie.QueryBatch([0, 1], [0], [0], [0], 5))
+    assert list(cnt) == [1] * 5
