@@ -26,7 +26,7 @@ class GenieIndexInfo(ctypes.Structure):
 
 class GenieBatchConfig(ctypes.Structure):
     _fields_ = [("max_queries", I32), ("max_items", I64), ("max_k", U32), ("use_graph", I32),
-                ("autotune", I32)]
+                ("max_units", I64)]
 
 
 class GenieTuning(ctypes.Structure):

@@ -9,9 +9,10 @@ from . import _lib
 
 
 class Batch:
-    def __init__(self, table, max_queries, max_items, max_k, use_graph=True):
+    def __init__(self, table, max_queries, max_items, max_k, use_graph=True, max_units=0):
         from . import _check, lib
-        cfg = _lib.GenieBatchConfig(int(max_queries), int(max_items), int(max_k), int(bool(use_graph)), 0)
+        cfg = _lib.GenieBatchConfig(int(max_queries), int(max_items), int(max_k), int(bool(use_graph)),
+                                    int(max_units))
         h = ctypes.c_void_p()
         _check(lib().genie_batch_create(table.handle, ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h

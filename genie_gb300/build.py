@@ -22,6 +22,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--extended-lambda", "-Xcompiler", "-fPIC",
               "-I" + os.path.join(ROOT, "include")] + ARCH
 CXX_FLAGS = ["-std=c++17", "-O3", "-fPIC", "-I" + os.path.join(ROOT, "include")]
+# GENIE_CHECKED=1 builds the bounds-checked variant (index reports instead of faults)
+if os.environ.get("GENIE_CHECKED") == "1":
+    NVCC_FLAGS.append("-DGG_CHECKED")
 
 
 def _nvcc():

@@ -219,7 +219,8 @@ int genie_batch_create(genie_index *ix, const genie_batch_config *cfg, genie_bat
     b->cfg = *cfg;
     b->tuning = ix->tuning;
     const int64_t Q = cfg->max_queries, I = cfg->max_items > 0 ? cfg->max_items : 1, K = (int64_t)Q * cfg->max_k;
-    cudaError_t e = b->ws.reserve(Q, I, K);
+    const int64_t U = cfg->max_units > 0 ? cfg->max_units : 16 * I;
+    cudaError_t e = b->ws.reserve(Q, I, U, K);
     if (!e) e = b->dyn.reserve(16);
     if (!e) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
     if (!e) e = cudaEventCreate(&b->ev0);

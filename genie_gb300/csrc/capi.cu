@@ -6,6 +6,7 @@
 
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <fstream>
 #include <string>
@@ -62,7 +63,7 @@ DeviceContext &device_context(int dev) {
     return c;
 }
 
-cudaError_t Workspace::reserve(int64_t Q, int64_t items, int64_t sumk) {
+cudaError_t Workspace::reserve(int64_t Q, int64_t items, int64_t units, int64_t sumk) {
     cudaError_t e;
 #define RES(buf, n) if ((e = buf.reserve((size_t)(n))) != cudaSuccess) return e
     RES(item_off, (Q + 1) * 8);
@@ -73,9 +74,13 @@ cudaError_t Workspace::reserve(int64_t Q, int64_t items, int64_t sumk) {
     RES(weighted, Q + 16);
     RES(k, Q * 4 + 16);
     RES(out_off, (Q + 1) * 8);
-    RES(span_start, items * 8 + 16);
-    RES(span_len, items * 8 + 16);
-    RES(inc, items * 4 + 16);
+    RES(item_k0, items * 8 + 16);
+    RES(item_nk, items * 4 + 16);
+    RES(item_inc, items * 4 + 16);
+    RES(q_unit_off, (Q + 1) * 8 + 16);
+    RES(span_start, units * 8 + 16);
+    RES(span_len, units * 8 + 16);
+    RES(inc, units * 4 + 16);
     RES(qinfo, Q * sizeof(QInfo) + 16);
     RES(work, (size_t)kNumLists * Q * kMaxParts * sizeof(uint2) + 16);
     RES(ctr, kCtrWords * 4);
@@ -96,7 +101,8 @@ cudaError_t Workspace::reserve(int64_t Q, int64_t items, int64_t sumk) {
 }
 
 void Workspace::release() {
-    DevBuf *all[] = {&item_off, &dim, &low, &up, &weight, &weighted, &k, &out_off, &span_start,
+    DevBuf *all[] = {&item_off, &dim, &low, &up, &weight, &weighted, &k, &out_off, &item_k0, &item_nk,
+                     &item_inc, &q_unit_off, &span_start,
                      &span_len, &inc, &qinfo, &work, &ctr, &qstate, &done, &part_cnt, &scratch,
                      &out_ids, &out_counts, &out_scores};
     for (DevBuf *b : all) b->release();
@@ -104,6 +110,10 @@ void Workspace::release() {
 
 Work Workspace::view(int64_t Q, bool scores) const {
     Work w;
+    w.item_k0 = (int64_t *)item_k0.p;
+    w.item_nk = (uint32_t *)item_nk.p;
+    w.item_inc = (uint32_t *)item_inc.p;
+    w.q_unit_off = (int64_t *)q_unit_off.p;
     w.span_start = (int64_t *)span_start.p;
     w.span_len = (int64_t *)span_len.p;
     w.inc = (uint32_t *)inc.p;
@@ -118,6 +128,10 @@ Work Workspace::view(int64_t Q, bool scores) const {
     w.out_ids = (uint32_t *)out_ids.p;
     w.out_counts = (uint32_t *)out_counts.p;
     w.out_scores = scores ? (float *)out_scores.p : nullptr;
+    w.units_cap = (int64_t)(span_len.bytes / 8);
+    w.items_cap = (int64_t)(item_nk.bytes / 4);
+    w.q_cap = Q;
+    w.out_cap = (int64_t)(out_ids.bytes / 4);
     return w;
 }
 
@@ -154,9 +168,30 @@ int validate_queries(const genie_queries *q, std::vector<int64_t> &out_off, int6
     return GENIE_OK;
 }
 
+// Exact number of (dim,value) lists the batch's items cover (one unit each).
+int64_t count_units(const HostIndex &h, const genie_queries *q) {
+    int64_t units = 0;
+    const int64_t n = q->n_queries > 0 ? q->item_off[q->n_queries] : 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const int32_t d = q->dim[i];
+        if (d < 0 || d >= h.n_dims) continue;
+        const int64_t lo = std::max<int64_t>(q->low[i], h.dim_min[d]);
+        const int64_t hi = std::min<int64_t>(q->up[i], h.dim_max[d]);
+        if (hi >= lo) units += hi - lo + 1;
+    }
+    return units;
+}
+
 int check_device_error(uint32_t err) {
+    unsigned long long oob[4];
+    read_oob(oob);
+    if (oob[0])
+        return fail(GENIE_ERR_CUDA, "checked build: index out of bounds at site %llu: %llu >= %llu (block %llu thread %llu)",
+                    oob[0], oob[1], oob[2], oob[3] >> 32, oob[3] & 0xffffffffull);
     if (err & kErrWeight) return fail(GENIE_ERR_INVALID_ARG, "a weighted query holds a weight that is not finite and > 0");
     if (err & kErrCapacity) return fail(GENIE_ERR_INVALID_ARG, "k outside [1, %d]", kMaxK);
+    if (err & kErrUnits)
+        return fail(GENIE_ERR_INVALID_ARG, "the batch's items cover more (dim,value) lists than its unit capacity");
     if (err) return fail(GENIE_ERR_CUDA, "device reported error flags 0x%x", err);
     return GENIE_OK;
 }
@@ -194,6 +229,7 @@ int upload_index(genie_index *ix) {
     d.n_ids = ix->n_ids;
     d.n_dims = h.n_dims;
     d.mult_max = h.mult_max;
+    d.is_bag = ix->is_bag ? 1 : 0;
     return GENIE_OK;
 }
 
@@ -229,7 +265,7 @@ int run_search(genie_index *ix, const genie_queries *q, const std::vector<int64_
     const int64_t Q = q->n_queries;
     const int64_t sumk = out_off[Q];
     Workspace &ws = ix->ws;
-    cudaError_t e = ws.reserve(Q, n_items, sumk);
+    cudaError_t e = ws.reserve(Q, n_items, count_units(ix->host, q), sumk);
     if (e) return cuda_fail(e, "search workspace");
     cudaStream_t s = ix->stream;
 #define H2D(dst, src, n) if ((n) > 0 && (e = cudaMemcpyAsync(dst, src, (size_t)(n), cudaMemcpyHostToDevice, s))) return cuda_fail(e, "query upload")

@@ -37,17 +37,19 @@ DeviceContext &device_context(int dev);
 // part scratch, results), grown on demand.
 struct Workspace {
     DevBuf item_off, dim, low, up, weight, weighted, k, out_off;
+    DevBuf item_k0, item_nk, item_inc, q_unit_off;
     DevBuf span_start, span_len, inc, qinfo, work, ctr, qstate, done, part_cnt, scratch;
     DevBuf out_ids, out_counts, out_scores;
     bool done_zeroed = false;
     int64_t done_q = 0;
-    cudaError_t reserve(int64_t Q, int64_t items, int64_t sumk);
+    cudaError_t reserve(int64_t Q, int64_t items, int64_t units, int64_t sumk);
     void release();
     Work view(int64_t Q, bool scores) const;
 };
 
 int validate_queries(const genie_queries *q, std::vector<int64_t> &out_off, int64_t &n_items);
 int check_device_error(uint32_t err);
+int64_t count_units(const HostIndex &h, const genie_queries *q);
 
 }  // namespace gg
 

@@ -1,0 +1,201 @@
+// codecs.cuh -- warp-level decoders of the reference posting-list codecs,
+// emitting values in sequence order straight into the counting loop.
+//
+// Formats (byte-compatible with the reference's host encoders):
+//   COPY     words are the values                       (DeviceCodecs.h:113-154)
+//   DELTA    words are differences, first from 0        (DeviceCodecs.cu:89-139)
+//   BP32     [n][w0<<24|w1<<16|w2<<8|w3][w0 words]..[w3 words] per 128 values;
+//            value j of a 32-value miniblock sits at bits [j*w, j*w+w), LSB
+//            first; a short tail packs ceil(rem/32) zero-padded miniblocks
+//                                                      (DeviceBitPackingCodec.cu:15-58)
+//   VARINT   7-bit groups, low first, the LAST byte of a value has bit 7 set,
+//            zero-padded to whole words                 (DeviceVarintCodec.cu:14-78)
+//   COMP(BP32,C2)  [len1][BP32 over floor(n/8)*8 values][C2 over the rest]
+//                                                      (DeviceCompositeCodec.cu:28-58)
+//   SERIAL(C1,C2)  C2 decoded first, then C1            (DeviceSerialCodec.cu:67-137)
+//
+// The reference decodes one segment per 256-thread block through shared
+// memory with a sequential header parse on thread 0
+// (DeviceBitPackingCodec.cu:160-200) and block-wide scans (utility/scan.cu).
+// Here one warp decodes one segment: miniblock offsets come from the header
+// bytes, varint boundaries from the terminal bits of each lane's word, and
+// delta runs as a warp prefix sum with a carry.
+#pragma once
+#include "codecs_host.h"
+#include "device.cuh"
+
+namespace gg {
+
+// Emits a group of values: lane l holds `cnt` values val[0..cnt) whose
+// sequence positions are base + before(l) + 0..cnt-1 (before = exclusive
+// prefix of cnt over lanes).  The emitter applies the delta stages in
+// sequence order and hands each value to `visit`.
+template <class V>
+struct Emitter {
+    int deltas;
+    uint32_t carry1 = 0, carry2 = 0;
+    uint32_t emitted = 0;      // values emitted so far (sequence position of the next)
+    V &visit;
+    __device__ Emitter(int d, V &v) : deltas(d), visit(v) {}
+    __device__ __forceinline__ void emit(const uint32_t *val, int cnt) {
+        // sequence position of this lane's first value
+        const uint32_t cincl = warp_incl_scan((uint32_t)cnt);
+        const uint32_t pos0 = emitted + cincl - (uint32_t)cnt;
+        emitted += __shfl_sync(0xffffffffu, cincl, 31);
+        // stage 1: inclusive running sum within the lane, then across lanes
+        uint32_t loc[4];
+        uint32_t s = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j < cnt) s += val[j];
+            loc[j] = s;
+        }
+        if (deltas == 0) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (j < cnt) visit(val[j], pos0 + j);
+            return;
+        }
+        uint32_t incl = warp_incl_scan(s);
+        uint32_t pre = carry1 + incl - s;
+        carry1 += __shfl_sync(0xffffffffu, incl, 31);
+        uint32_t v1[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v1[j] = pre + loc[j];
+        if (deltas == 1) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (j < cnt) visit(v1[j], pos0 + j);
+            return;
+        }
+        // stage 2 (SERIAL_DELTA_DELTA)
+        uint32_t s2 = 0, loc2[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (j < cnt) s2 += v1[j];
+            loc2[j] = s2;
+        }
+        uint32_t incl2 = warp_incl_scan(s2);
+        uint32_t pre2 = carry2 + incl2 - s2;
+        carry2 += __shfl_sync(0xffffffffu, incl2, 31);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j < cnt) visit(pre2 + loc2[j], pos0 + j);
+    }
+};
+
+// Words [w0, w1) as values, 32 per step.
+template <class E>
+__device__ __forceinline__ void dec_copy(const uint32_t *__restrict__ w, int64_t w0, int64_t w1, E &em) {
+    for (int64_t b = w0; b < w1; b += 32) {
+        int64_t i = b + lane_id();
+        uint32_t v[1] = {i < w1 ? __ldg(w + i) : 0u};
+        em.emit(v, i < w1 ? 1 : 0);
+    }
+}
+
+// One BP32 stream starting at word w0 ([n][blocks...]); returns the word
+// after it.
+template <class E>
+__device__ __forceinline__ int64_t dec_bp32(const uint32_t *__restrict__ w, int64_t w0, E &em) {
+    const uint32_t lane = lane_id();
+    const uint32_t n = __ldg(w + w0);
+    int64_t p = w0 + 1;
+    for (uint32_t done = 0; done < n; done += 128) {
+        const uint32_t hdr = __ldg(w + p);
+        const uint32_t rem = n - done;
+        const uint32_t howmany = rem >= 128 ? 4u : (rem + 31) / 32;
+        int64_t off = p + 1;
+        for (uint32_t mb = 0; mb < howmany; ++mb) {
+            const uint32_t b = (hdr >> (24 - 8 * mb)) & 255u;
+            const uint32_t idx = done + mb * 32 + lane;
+            uint32_t v = 0;
+            if (b == 32) {
+                v = __ldg(w + off + lane);
+            } else if (b > 0) {
+                const uint32_t bit = lane * b, wi = bit >> 5, sh = bit & 31;
+                const uint32_t lo = __ldg(w + off + wi);
+                const uint32_t hi = (sh + b > 32) ? __ldg(w + off + wi + 1) : 0u;
+                v = (uint32_t)((((uint64_t)hi << 32) | lo) >> sh) & ((1u << b) - 1u);
+            }
+            uint32_t vv[1] = {v};
+            em.emit(vv, idx < n ? 1 : 0);
+            off += b;
+        }
+        p = off;
+    }
+    return p;
+}
+
+// Varint bytes of words [w0, w1): a lane owns one word; each byte with bit 7
+// set ends a value of at most five bytes, so a value spans at most this word
+// and the previous one.
+template <class E>
+__device__ __forceinline__ void dec_varint(const uint32_t *__restrict__ w, int64_t w0, int64_t w1, E &em) {
+    const uint32_t lane = lane_id();
+    uint32_t prev_last = 0;            // previous chunk's last word
+    bool have_prev = false;
+    for (int64_t b = w0; b < w1; b += 32) {
+        const int64_t i = b + lane;
+        const uint32_t cur = i < w1 ? __ldg(w + i) : 0u;
+        uint32_t prv = __shfl_up_sync(0xffffffffu, cur, 1);
+        if (lane == 0) prv = have_prev ? prev_last : 0u;
+        const bool prv_valid = lane > 0 || have_prev;
+        // terminal flags of the 8-byte window [prv | cur]
+        const uint64_t win = ((uint64_t)cur << 32) | prv;
+        uint32_t vals[4];
+        int cnt = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int pos = 4 + j;                       // byte index in the window
+            const uint32_t byte = (uint32_t)(win >> (8 * pos)) & 255u;
+            if (!(byte & 0x80u)) continue;
+            // walk back to the byte after the previous terminal (<= 4 bytes)
+            int start = pos;
+            while (start > 0 && (pos - start) < 4) {
+                const uint32_t pb = (uint32_t)(win >> (8 * (start - 1))) & 255u;
+                if (pb & 0x80u) break;
+                if (start - 1 < 4 && !prv_valid) break;
+                --start;
+            }
+            uint32_t v = 0;
+            for (int t = pos; t >= start; --t) v = (v << 7) | ((uint32_t)(win >> (8 * t)) & 0x7Fu);
+            vals[cnt++] = v;
+        }
+        em.emit(vals, cnt);
+        prev_last = __shfl_sync(0xffffffffu, cur, 31);
+        have_prev = true;
+    }
+}
+
+// Decode one encoded segment (words [w0, w1)) and visit its values in order.
+template <class V>
+__device__ __forceinline__ void decode_segment(int codec, const uint32_t *__restrict__ w, int64_t w0, int64_t w1,
+                                               V &visit) {
+    int deltas, inner;
+    codec_parts(codec, deltas, inner);
+    Emitter<V> em(deltas, visit);
+    switch (inner) {
+    case kInnerCopy:
+        dec_copy(w, w0, w1, em);
+        break;
+    case kInnerBP32:
+        dec_bp32(w, w0, em);
+        break;
+    case kInnerVarint:
+        dec_varint(w, w0, w1, em);
+        break;
+    default: {     // composite: [len1][BP32 (len1 words)][tail]
+        const uint32_t len1 = __ldg(w + w0);
+        int64_t p = w0 + 1;
+        if (len1) dec_bp32(w, p, em);
+        p += len1;
+        if (p < w1) {
+            if (inner == kInnerCompCopy) dec_copy(w, p, w1, em);
+            else dec_varint(w, p, w1, em);
+        }
+    }
+    }
+}
+
+}  // namespace gg

@@ -23,7 +23,7 @@ constexpr int kCandCap = 2048;       // candidate buffer of the top-k selection
 
 enum : uint8_t { kClsNone = 0, kClsSparse = 1, kClsDense = 2 };
 enum : uint8_t { kFlagWeighted = 1, kFlagSmallCount = 2, kFlagRetry = 4, kFlagPacked = 8 };
-enum : uint32_t { kErrWeight = 1, kErrOverflow = 2, kErrCapacity = 4 };
+enum : uint32_t { kErrWeight = 1, kErrOverflow = 2, kErrCapacity = 4, kErrUnits = 8 };
 
 struct DevIndex {
     const uint32_t *ids;
@@ -35,14 +35,15 @@ struct DevIndex {
     int64_t n_ids;
     int32_t n_dims;
     int32_t mult_max;
+    int32_t is_bag;
     // compressed layout (codec != 0)
     int32_t codec;
     int32_t max_seg;
-    const uint32_t *words;
-    const int64_t *key_seg;
-    const int64_t *seg_word_off;
-    const uint32_t *seg_first;
-    const uint32_t *seg_len;
+    const uint32_t *words;         // encoded segments
+    const int64_t *key_seg;        // [n_keys+1] first segment of each key
+    const int64_t *seg_word_off;   // [n_segs+1] first word of each segment
+    const uint32_t *seg_first;     // [n_segs] first id of each segment (skip pointer)
+    const int64_t *seg_pos;        // [n_segs+1] posting position of each segment
 };
 
 struct DevQueries {
@@ -64,7 +65,9 @@ struct DevQueries {
 // Per-query plan written by k_plan.
 struct QInfo {
     int64_t total;      // posting ids touched (sum of span lengths)
+    int64_t unit0;      // first unit (one sorted posting list of one item)
     int64_t item0;      // first item
+    int32_t n_units;
     int32_t n_items;
     uint32_t k;
     int32_t scale;      // fixed-point exponent of a weighted query
@@ -94,9 +97,13 @@ constexpr int kCtrWords = 2 * kNumLists + 2;
 
 // Device work state of one search (all arrays sized for the batch).
 struct Work {
-    int64_t *span_start;   // [items] global position of the item's span
-    int64_t *span_len;     // [items]
-    uint32_t *inc;         // [items] increment per match (1, or fixed-point weight)
+    int64_t *item_k0;      // [items] first key an item covers
+    uint32_t *item_nk;     // [items] keys it covers (0: matches nothing)
+    uint32_t *item_inc;    // [items] increment per match (1, or fixed-point weight)
+    int64_t *q_unit_off;   // [Q+1] unit count, then first unit, of every query
+    int64_t *span_start;   // [units] start of the unit's sorted list (or first segment)
+    int64_t *span_len;     // [units] its length (or segment count)
+    uint32_t *inc;         // [units] increment per match
     QInfo *qinfo;          // [Q]
     uint2 *work;           // [kNumLists][Q*kMaxParts] (query, part)
     int64_t work_stride;   // Q*kMaxParts
@@ -108,7 +115,33 @@ struct Work {
     uint32_t *out_ids;
     uint32_t *out_counts;
     float *out_scores;     // may be null
+    // capacities (units_cap is enforced; the others bound the checked build)
+    int64_t units_cap;
+    int64_t items_cap;
+    int64_t q_cap;
+    int64_t out_cap;
 };
+
+// ---------------------------------------------------------------- checked builds
+//
+// Built with -DGG_CHECKED, every index below is bounds-checked; the first
+// violation is recorded (site, index, bound) in gg_oob and the access is
+// skipped, so a faulty index shows up as a report instead of a memory fault.
+#ifdef GG_CHECKED
+// one copy per translation unit: only match.cu's kernels report into theirs
+static __device__ unsigned long long gg_oob[4];
+__device__ __forceinline__ bool gg_report(uint32_t site, uint64_t idx, uint64_t n) {
+    if (atomicCAS(&gg_oob[0], 0ull, (unsigned long long)site) == 0ull) {
+        gg_oob[1] = idx;
+        gg_oob[2] = n;
+        gg_oob[3] = ((unsigned long long)blockIdx.x << 32) | threadIdx.x;
+    }
+    return false;
+}
+#define GG_OK(idx, n, site) (((uint64_t)(idx) < (uint64_t)(n)) || gg::gg_report((site), (uint64_t)(idx), (uint64_t)(n)))
+#else
+#define GG_OK(idx, n, site) true
+#endif
 
 // ---------------------------------------------------------------- helpers
 
@@ -217,6 +250,7 @@ __device__ __forceinline__ void write_results(const Work &W, int64_t out_off, ui
                                               const uint64_t *sorted, uint32_t n, bool weighted,
                                               int32_t scale) {
     for (uint32_t j = threadIdx.x; j < k; j += blockDim.x) {
+        if (!GG_OK(out_off + j, W.out_cap, 4)) continue;
         uint32_t id = 0, cnt = 0;
         float sc = 0.0f;
         if (j < n) {

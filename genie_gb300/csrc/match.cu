@@ -7,6 +7,7 @@
 // and extract_index_and_count (knn.cu:47-55).  The reference counts every
 // posting id with a global-memory atomicCAS on a packed per-query bitmap and
 // probes a per-query global hash; here every count lives in shared memory.
+#include "codecs.cuh"
 #include "match.cuh"
 #include "select.cuh"
 
@@ -15,12 +16,29 @@
 
 namespace gg {
 
-// ------------------------------------------------------------------ plan
+// First out-of-bounds report of a checked build (all zero otherwise).
+void read_oob(unsigned long long out[4]) {
+    out[0] = out[1] = out[2] = out[3] = 0;
+#ifdef GG_CHECKED
+    cudaMemcpyFromSymbol(out, gg_oob, sizeof(unsigned long long) * 4);
+#endif
+}
 
-// One warp per query: items -> spans (Query::build, query/query.cc:273-333),
-// per-item increments, the fixed-point scale of weighted queries, and the
-// sparse/dense decision with the number of id-range parts.
-__global__ void __launch_bounds__(256) k_plan(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+// ------------------------------------------------------------------ plan
+//
+// Query compile on the device, in three launches:
+//   k_plan_items  one warp per query: clamp every item (Query::attr /
+//                 Query::build, query/query.cc:87-113, 273-333), count the
+//                 (dim,value) lists it covers, the posting ids it touches,
+//                 and the fixed-point scale of a weighted query;
+//   k_unit_scan   one CTA: exclusive scan of the per-query list counts;
+//   k_plan_units  one warp per query: one unit per covered list (a sorted
+//                 posting list, or the segment range of a compressed one),
+//                 then the sparse/dense decision and the work lists.
+// A range item covers several lists whose concatenation is not sorted, so
+// every later search inside a span happens per unit.
+
+__global__ void __launch_bounds__(256) k_plan_items(DevIndex ix, DevQueries Q, Work W, Tuning T) {
     const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
     if (q >= nq) return;
@@ -47,44 +65,120 @@ __global__ void __launch_bounds__(256) k_plan(DevIndex ix, DevQueries Q, Work W,
         bad = __shfl_sync(0xffffffffu, bad, 0);
         if (bad && lane == 0) atomicOr(&W.ctr[kCtrError], kErrWeight);
     }
-    int64_t total = 0;
+    int64_t total = 0, units = 0;
     for (int64_t i = i0 + lane; i < i1; i += 32) {
+        if (!GG_OK(i, W.items_cap, 7)) break;
         int32_t d = Q.dim[i], lo = Q.low[i], hi = Q.up[i];
-        int64_t start = 0, end = 0;
+        int64_t k0 = 0, nk = 0;
         if (d >= 0 && d < ix.n_dims) {
             int32_t mn = ix.dim_min[d], mx = ix.dim_max[d];
             if (!(lo > hi || lo > mx || hi < mn)) {
                 if (lo < mn) lo = mn;
                 if (hi > mx) hi = mx;
-                int64_t k0 = ix.key_base[d] + ((int64_t)lo - mn);
-                int64_t k1 = ix.key_base[d] + ((int64_t)hi - mn) + 1;
-                start = ix.key_off[k0];
-                end = ix.key_off[k1];
+                k0 = ix.key_base[d] + ((int64_t)lo - mn);
+                nk = (int64_t)hi - lo + 1;
+                total += ix.key_off[k0 + nk] - ix.key_off[k0];
             }
         }
-        W.span_start[i] = start;
-        W.span_len[i] = end - start;
+        W.item_k0[i] = k0;
+        W.item_nk[i] = nk;
         uint32_t inc = 1;
         if (weighted) inc = (uint32_t)__double2ll_rn(ldexp((double)Q.weight[i], scale));
-        W.inc[i] = inc;
-        total += end - start;
+        W.item_inc[i] = inc;
+        units += nk;
     }
     total = (int64_t)warp_sum_u64((uint64_t)total);
-    if (lane == 0) {
+    units = (int64_t)warp_sum_u64((uint64_t)units);
+    if (lane == 0 && GG_OK(q, W.q_cap, 12)) {
         QInfo qi;
         qi.total = total;
+        qi.unit0 = 0;
+        qi.n_units = units;
         qi.item0 = i0;
         qi.n_items = m;
         qi.k = k;
         qi.scale = scale;
         qi.flags = weighted ? kFlagWeighted : 0;
-        const bool small = !weighted && (int64_t)m * ix.mult_max <= 255;
-        if (small) qi.flags |= kFlagSmallCount;
+        // bound on any object's count: one match per item on a one-value-per-dim
+        // table; on a bag table, every covered list may repeat the object
+        const int64_t bound = ix.is_bag ? units * ix.mult_max : (int64_t)m;
+        if (!weighted && bound <= 255) qi.flags |= kFlagSmallCount;
         qi.parts = 1;
         qi.cls = kClsNone;
-        int list = -1;
+        W.qinfo[q] = qi;
+        W.q_unit_off[q] = units;
+        W.done[q] = 0;
+        W.qstate[q] = 0;
         if (k == 0 || k > (uint32_t)kMaxK) atomicOr(&W.ctr[kCtrError], kErrCapacity);
-        else if (total > 0) {
+    }
+}
+
+// Exclusive scan of the per-query unit counts (one CTA, any number of queries).
+__global__ void __launch_bounds__(1024) k_unit_scan(DevQueries Q, Work W) {
+    __shared__ uint32_t s_tmp[48];
+    __shared__ int64_t s_carry;
+    const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
+    if (threadIdx.x == 0) s_carry = 0;
+    __syncthreads();
+    for (int64_t b = 0; b < nq; b += blockDim.x) {
+        const int64_t q = b + threadIdx.x;
+        const int64_t v = q < nq ? W.q_unit_off[q] : 0;
+        // units per query fit 32 bits; the running offset is 64-bit
+        uint32_t tot = 0;
+        const uint32_t ex = block_excl_scan((uint32_t)v, s_tmp, &tot);
+        const int64_t off = s_carry + ex;
+        if (q < nq) {
+            W.q_unit_off[q] = off;
+            W.qinfo[q].unit0 = off;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        W.q_unit_off[nq] = s_carry;
+        if (s_carry > W.units_cap) atomicOr(&W.ctr[kCtrError], kErrUnits);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_plan_units(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
+    if (q >= nq) return;
+    const uint32_t lane = lane_id();
+    QInfo qi = W.qinfo[q];
+    const bool fits = W.q_unit_off[nq] <= W.units_cap;
+    if (fits) {
+        int64_t base = qi.unit0;
+        const int64_t i1 = qi.item0 + qi.n_items;
+        for (int64_t c = qi.item0; c < i1; c += 32) {
+            const int64_t i = c + lane;
+            const int64_t nk = i < i1 ? (int64_t)W.item_nk[i] : 0;
+            // units fit 32 bits within one warp step
+            const uint32_t incl = warp_incl_scan((uint32_t)nk);
+            const int64_t u0 = base + incl - nk;
+            if (nk) {
+                const int64_t k0 = W.item_k0[i];
+                const uint32_t inc = W.item_inc[i];
+                for (int64_t j = 0; j < nk; ++j) {
+                    const int64_t u = u0 + j, key = k0 + j;
+                    if (!GG_OK(u, W.units_cap, 14)) break;
+                    const int64_t a = ix.codec ? ix.key_seg[key] : ix.key_off[key];
+                    const int64_t e = ix.codec ? ix.key_seg[key + 1] : ix.key_off[key + 1];
+                    W.span_start[u] = a;
+                    W.span_len[u] = e - a;
+                    W.inc[u] = inc;
+                }
+            }
+            base += __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+    if (lane == 0) {
+        const uint32_t k = qi.k;
+        const bool small = (qi.flags & kFlagSmallCount) != 0;
+        const int64_t total = qi.total;
+        int list = -1;
+        if (fits && k >= 1 && k <= (uint32_t)kMaxK && total > 0) {
             const bool packed = small && ix.n_objects <= (int64_t)(1u << 24);
             const int64_t slots = packed ? T.sparse_slots_packed : T.sparse_slots_wide;
             const int64_t cap = slots * 3 / 4;
@@ -107,19 +201,19 @@ __global__ void __launch_bounds__(256) k_plan(DevIndex ix, DevQueries Q, Work W,
             }
         }
         W.qinfo[q] = qi;
-        W.done[q] = 0;
-        W.qstate[q] = 0;
         if (list >= 0) {
             uint2 *wl = W.work + (size_t)list * W.work_stride;
-            uint32_t base = atomicAdd(&W.ctr[2 * list], (uint32_t)qi.parts);
-            for (uint32_t p = 0; p < qi.parts; ++p) wl[base + p] = make_uint2((uint32_t)q, p);
+            uint32_t b = atomicAdd(&W.ctr[2 * list], (uint32_t)qi.parts);
+            for (uint32_t p = 0; p < qi.parts; ++p)
+                if (GG_OK(b + p, W.work_stride, 8)) wl[b + p] = make_uint2((uint32_t)q, p);
         }
     }
     // queries without any matching posting: padded results right away
     __syncwarp();
-    if (k >= 1 && k <= (uint32_t)kMaxK && total == 0) {
+    if (qi.k >= 1 && qi.k <= (uint32_t)kMaxK && qi.total == 0) {
         const int64_t o = Q.out_off[q];
-        for (uint32_t j = lane; j < k; j += 32) {
+        for (uint32_t j = lane; j < qi.k; j += 32) {
+            if (!GG_OK(o + j, W.out_cap, 4)) break;
             W.out_ids[o + j] = 0;
             W.out_counts[o + j] = 0;
             if (W.out_scores) W.out_scores[o + j] = 0.0f;
@@ -141,8 +235,9 @@ struct ItemStage {
 // Warps take 256-position chunks of the flattened span list; each lane loads
 // 8 ids (coalesced within a span) before visiting them.
 template <class V>
-__device__ __forceinline__ void stream_ids(const uint32_t *__restrict__ ids, const ItemStage &st,
+__device__ __forceinline__ void stream_ids(const uint32_t *__restrict__ ids, int64_t n_ids, const ItemStage &st,
                                            uint32_t n_items, uint32_t F, V &&visit) {
+    (void)n_ids;
     const uint32_t lane = lane_id();
     const uint32_t nw = blockDim.x >> 5;
     for (uint32_t base = warp_id() * 256u; base < F; base += nw * 256u) {
@@ -163,16 +258,103 @@ __device__ __forceinline__ void stream_ids(const uint32_t *__restrict__ ids, con
             inc[j] = 0;
             v[j] = 0;
             if (f < F) {
-                while (st.flat[it + 1] <= f) ++it;
+                while (GG_OK(it + 1, n_items + 1, 11) && st.flat[it + 1] <= f) ++it;
                 int64_t pos = st.start[it] + (int64_t)(f - st.flat[it]);
-                v[j] = __ldg(ids + pos);
-                inc[j] = st.inc[it];
+                if (GG_OK(pos, n_ids, 1)) {
+                    v[j] = __ldg(ids + pos);
+                    inc[j] = st.inc[it];
+                }
             }
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j)
             if (inc[j]) visit(v[j], inc[j]);
     }
+}
+
+// Compressed index: every warp decodes whole segments (<= 1024 ids) and
+// visits the ids inside [lo, hi).  Decoding is fused into counting: ids go
+// from the unpacked words straight to the shared-memory counters.
+template <class V>
+__device__ __forceinline__ void stream_segments(const DevIndex &ix, const ItemStage &st, uint32_t n_items,
+                                                uint32_t F, uint32_t lo, uint32_t hi, V &&visit) {
+    const uint32_t nw = blockDim.x >> 5;
+    for (uint32_t f = warp_id(); f < F; f += nw) {
+        uint32_t a = 0, b = n_items;       // last item with flat <= f
+        while (a < b) {
+            uint32_t mid = (a + b + 1) >> 1;
+            if (st.flat[mid] <= f) a = mid; else b = mid - 1;
+        }
+        const int64_t seg = st.start[a] + (int64_t)(f - st.flat[a]);
+        const uint32_t inc = st.inc[a];
+        auto v = [&](uint32_t id, uint32_t) {
+            if (id >= lo && id < hi && inc) visit(id, inc);
+        };
+        decode_segment(ix.codec, ix.words, ix.seg_word_off[seg], ix.seg_word_off[seg + 1], v);
+    }
+}
+
+template <class V>
+__device__ __forceinline__ void stream_units(const DevIndex &ix, const ItemStage &st, uint32_t n_items, uint32_t F,
+                                             uint32_t lo, uint32_t hi, V &&visit) {
+    if (ix.codec) stream_segments(ix, st, n_items, F, lo, hi, visit);
+    else stream_ids(ix.ids, ix.n_ids, st, n_items, F, visit);
+}
+
+// First unit (posting position, or segment of a compressed index) of the
+// range [s0, e0) that can hold an id >= x.
+__device__ __forceinline__ int64_t first_unit(const DevIndex &ix, int64_t s0, int64_t e0, uint32_t x) {
+    if (!ix.codec) return lower_bound_u32(ix.ids, s0, e0, x);
+    int64_t a = lower_bound_u32(ix.seg_first, s0, e0, x);
+    return a > s0 ? a - 1 : a;
+}
+
+// Stage items [c0, c0+mc) of a query restricted to the ids [lo, hi): posting
+// positions (or, for a compressed index, segment indices) in st.start/len,
+// increments in st.inc, the exclusive prefix of len in st.flat.  cut_lo /
+// cut_hi request the binary searches for lo / hi.  Returns an upper bound on
+// the posting ids staged (block-uniform).
+__device__ uint64_t stage_range(const DevIndex &ix, const Work &W, const QInfo &qi, int32_t c0, int32_t mc,
+                                bool cut_lo, bool cut_hi, uint32_t lo, uint32_t hi, ItemStage &st,
+                                SelectScratch &ss) {
+    const uint32_t tid = threadIdx.x;
+    uint32_t len = 0;
+    uint64_t ids = 0;
+    if (tid == 0) ss.tot64 = 0;
+    if ((int32_t)tid < mc && GG_OK(qi.unit0 + c0 + tid, W.units_cap, 9)) {
+        const int64_t it = qi.unit0 + c0 + tid;
+        const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
+        int64_t a = s0, b = e0;
+        if (e0 > s0) {
+            if (!ix.codec) {
+                if (cut_lo) a = lower_bound_u32(ix.ids, s0, e0, lo);
+                if (cut_hi) b = lower_bound_u32(ix.ids, a, e0, hi);
+                ids = (uint64_t)(b - a);
+            } else {
+                if (cut_lo) {       // the segment before the first one starting at >= lo may reach lo
+                    a = lower_bound_u32(ix.seg_first, s0, e0, lo);
+                    if (a > s0) --a;
+                }
+                if (cut_hi) b = lower_bound_u32(ix.seg_first, a, e0, hi);
+                ids = (uint64_t)(ix.seg_pos[b] - ix.seg_pos[a]);
+            }
+        }
+        st.start[tid] = a;
+        st.inc[tid] = W.inc[it];
+        len = (uint32_t)(b - a);
+        st.len[tid] = len;
+    }
+    uint32_t tot = 0;
+    const uint32_t off = block_excl_scan(len, ss.tmp, &tot);
+    if ((int32_t)tid < mc) st.flat[tid] = off;
+    if (tid == 0) st.flat[mc] = tot;
+    if (!ix.codec) return tot;
+    ids = warp_sum_u64(ids);
+    if (lane_id() == 0 && ids) atomicAdd((unsigned long long *)&ss.tot64, (unsigned long long)ids);
+    __syncthreads();
+    const uint64_t r = ss.tot64;
+    __syncthreads();
+    return r;
 }
 
 // Scratch / merge of a query's parts.  Part p of query q keeps its sorted
@@ -188,6 +370,7 @@ struct MergeSet {
             for (uint32_t b = 0; b < n; b += blockDim.x) {
                 uint32_t i = b + threadIdx.x;
                 bool act = i < n;
+                act = act && GG_OK((size_t)p * k + i, (size_t)kMaxParts * k, 6);
                 uint64_t key = act ? __ldcg(keys + (size_t)p * k + i) : 0ull;
                 f(act, key_prim(key), key_id(key));
             }
@@ -211,7 +394,8 @@ __device__ void convert_to_dense(const DevIndex &ix, const Work &W, const Tuning
     const int list = small ? kListDenseSmall : kListDenseWide;
     uint2 *wl = W.work + (size_t)list * W.work_stride;
     uint32_t base = atomicAdd(&W.ctr[2 * list], (uint32_t)pd);
-    for (uint32_t p = 0; p < pd; ++p) wl[base + p] = make_uint2(q, p);
+    for (uint32_t p = 0; p < pd; ++p)
+        if (GG_OK(base + p, W.work_stride, 13)) wl[base + p] = make_uint2(q, p);
 }
 
 // Finish one part: publish its keys, and let the last part merge them.
@@ -225,7 +409,9 @@ __device__ void finish_part(const DevIndex &ix, const Work &W, const Tuning &T, 
         return;
     }
     uint64_t *dst = W.scratch + (size_t)out_off * kMaxParts + (size_t)p * qi.k;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) __stcg(dst + i, cand[i]);
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        if (GG_OK((size_t)out_off * kMaxParts + (size_t)p * qi.k + i, (size_t)W.out_cap * kMaxParts, 5))
+            __stcg(dst + i, cand[i]);
     if (threadIdx.x == 0) {
         __stcg(W.part_cnt + (size_t)q * kMaxParts + p, failed ? 0u : n);
         if (failed) atomicOr(&W.qstate[q], 1u);
@@ -313,37 +499,20 @@ __global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Wo
         if (w >= *(volatile uint32_t *)&W.ctr[2 * list]) break;
         const uint2 wk = W.work[(size_t)list * W.work_stride + w];
         const uint32_t q = wk.x, p = wk.y;
+        if (!GG_OK(q, W.q_cap, 12)) continue;
         const QInfo qi = W.qinfo[q];
         const uint32_t P = qi.parts;
         const uint32_t id_lo = (uint32_t)(((uint64_t)ix.n_objects * p) / P);
         const uint32_t id_hi = (uint32_t)(((uint64_t)ix.n_objects * (p + 1)) / P);
 
-        // pass 1: part size (sum of sub-span lengths) bounds the distinct ids
+        // pass 1: part size (posting ids in the part's sub-spans) bounds the distinct ids
         uint64_t part_total = 0;
-        for (int32_t c0 = 0; c0 < qi.n_items; c0 += kItemChunk) {
-            const int32_t mc = min(kItemChunk, qi.n_items - c0);
-            uint32_t len = 0;
-            if ((int32_t)tid < mc) {
-                const int64_t it = qi.item0 + c0 + tid;
-                const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
-                int64_t a = s0, b = e0;
-                if (P > 1 && e0 > s0) {
-                    a = p == 0 ? s0 : lower_bound_u32(ix.ids, s0, e0, id_lo);
-                    b = p == P - 1 ? e0 : lower_bound_u32(ix.ids, a, e0, id_hi);
-                }
-                st.start[tid] = a;
-                st.inc[tid] = W.inc[it];
-                len = (uint32_t)(b - a);
-                st.len[tid] = len;
-            }
-            uint32_t tot = 0;
-            uint32_t off = block_excl_scan(len, ss.tmp, &tot);
-            if ((int32_t)tid < mc) st.flat[tid] = off;
-            if (tid == 0) st.flat[mc] = tot;
-            part_total += tot;
-            if (qi.n_items > kItemChunk) __syncthreads();
+        for (int32_t c0 = 0; c0 < qi.n_units; c0 += kItemChunk) {
+            const int32_t mc = min(kItemChunk, qi.n_units - c0);
+            part_total += stage_range(ix, W, qi, c0, mc, P > 1 && p > 0, P > 1 && p < P - 1, id_lo, id_hi, st, ss);
+            if (qi.n_units > kItemChunk) __syncthreads();
         }
-        const bool single = qi.n_items <= kItemChunk;
+        const bool single = qi.n_units <= kItemChunk;
         const bool overflow = part_total > (uint64_t)slots_max * 3 / 4;
         uint64_t *cand_out = cand;
         uint32_t nres = 0;
@@ -356,37 +525,19 @@ __global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Wo
             const uint32_t n4 = (cap * (PACKED ? 4 : 8) + 15) / 16;
             for (uint32_t i = tid; i < n4; i += blockDim.x) t4[i] = make_uint4(0, 0, 0, 0);
             __syncthreads();
-            for (int32_t c0 = 0; c0 < qi.n_items; c0 += kItemChunk) {
-                const int32_t mc = min(kItemChunk, qi.n_items - c0);
-                if (!single) {        // restage this chunk (pass 1 kept only the last)
-                    uint32_t len = 0;
-                    if ((int32_t)tid < mc) {
-                        const int64_t it = qi.item0 + c0 + tid;
-                        const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
-                        int64_t a = s0, b = e0;
-                        if (P > 1 && e0 > s0) {
-                            a = p == 0 ? s0 : lower_bound_u32(ix.ids, s0, e0, id_lo);
-                            b = p == P - 1 ? e0 : lower_bound_u32(ix.ids, a, e0, id_hi);
-                        }
-                        st.start[tid] = a;
-                        st.inc[tid] = W.inc[it];
-                        len = (uint32_t)(b - a);
-                    }
-                    uint32_t tot = 0;
-                    uint32_t off = block_excl_scan(len, ss.tmp, &tot);
-                    if ((int32_t)tid < mc) st.flat[tid] = off;
-                    if (tid == 0) st.flat[mc] = tot;
-                    __syncthreads();
-                } else {
-                    __syncthreads();
-                }
+            for (int32_t c0 = 0; c0 < qi.n_units; c0 += kItemChunk) {
+                const int32_t mc = min(kItemChunk, qi.n_units - c0);
+                if (!single)          // restage this chunk (pass 1 kept only the last)
+                    stage_range(ix, W, qi, c0, mc, P > 1 && p > 0, P > 1 && p < P - 1, id_lo, id_hi, st, ss);
+                __syncthreads();
                 const uint32_t F = st.flat[mc];
                 if (PACKED) {
                     uint32_t *tab = (uint32_t *)tab_raw;
-                    stream_ids(ix.ids, st, (uint32_t)mc, F, [&](uint32_t id, uint32_t) {
+                    stream_units(ix, st, (uint32_t)mc, F, id_lo, id_hi, [&](uint32_t id, uint32_t) {
                         uint32_t h = slot_of(id, cap);
                         const uint32_t want = (id << 8) | 1u;
                         for (uint32_t probe = 0; probe < cap; ++probe) {
+                            if (!GG_OK(h, cap, 2)) return;
                             uint32_t cur = tab[h];
                             if (cur == 0u) {
                                 uint32_t old = atomicCAS(&tab[h], 0u, want);
@@ -399,10 +550,11 @@ __global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Wo
                     });
                 } else {
                     unsigned long long *tab = (unsigned long long *)tab_raw;
-                    stream_ids(ix.ids, st, (uint32_t)mc, F, [&](uint32_t id, uint32_t inc) {
+                    stream_units(ix, st, (uint32_t)mc, F, id_lo, id_hi, [&](uint32_t id, uint32_t inc) {
                         uint32_t h = slot_of(id, cap);
                         const unsigned long long tag = (unsigned long long)(id + 1u) << 32;
                         for (uint32_t probe = 0; probe < cap; ++probe) {
+                            if (!GG_OK(h, cap, 2)) return;
                             unsigned long long cur = tab[h];
                             if (cur == 0ull) {
                                 unsigned long long old = atomicCAS(&tab[h], 0ull, tag | inc);
@@ -503,20 +655,20 @@ __global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Wo
         if (w >= *(volatile uint32_t *)&W.ctr[2 * list]) break;
         const uint2 wk = W.work[(size_t)list * W.work_stride + w];
         const uint32_t q = wk.x, p = wk.y;
+        if (!GG_OK(q, W.q_cap, 12)) continue;
         const QInfo qi = W.qinfo[q];
         const uint32_t P = qi.parts;
         const uint64_t N = (uint64_t)ix.n_objects;
         const uint64_t ntiles = (N + tile_cap - 1) / tile_cap;
         const uint64_t t0 = ntiles * p / P, t1 = ntiles * (p + 1) / P;
-        const bool single = qi.n_items <= kItemChunk;
+        const bool single = qi.n_units <= kItemChunk;
         const bool weighted = (qi.flags & kFlagWeighted) != 0;
         if (tid == 0) s_nS = 0;
         // cursor of every item at the part's first id
-        if (single && (int32_t)tid < qi.n_items) {
-            const int64_t it = qi.item0 + tid;
+        if (single && (int32_t)tid < qi.n_units) {
+            const int64_t it = qi.unit0 + tid;
             const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
-            cur[tid] = (t0 == 0 || e0 == s0) ? s0
-                                             : lower_bound_u32(ix.ids, s0, e0, (uint32_t)(t0 * tile_cap));
+            cur[tid] = (t0 == 0 || e0 == s0) ? s0 : first_unit(ix, s0, e0, (uint32_t)(t0 * tile_cap));
         }
         __syncthreads();
         for (uint64_t t = t0; t < t1; ++t) {
@@ -529,18 +681,19 @@ __global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Wo
             const uint32_t n4 = (n_pad * (SMALL ? 1 : 4)) / 16;
             for (uint32_t i = tid; i < n4; i += blockDim.x) c4[i] = make_uint4(0, 0, 0, 0);
             bool any_ids = false;
-            for (int32_t c0 = 0; c0 < qi.n_items; c0 += kItemChunk) {
-                const int32_t mc = min(kItemChunk, qi.n_items - c0);
+            for (int32_t c0 = 0; c0 < qi.n_units; c0 += kItemChunk) {
+                const int32_t mc = min(kItemChunk, qi.n_units - c0);
                 uint32_t len = 0;
                 if ((int32_t)tid < mc) {
-                    const int64_t it = qi.item0 + c0 + tid;
+                    const int64_t it = qi.unit0 + c0 + tid;
                     const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
-                    int64_t a = single ? cur[tid] : (t == 0 ? s0 : lower_bound_u32(ix.ids, s0, e0, tile_lo));
-                    int64_t b = (tile_hi >= N) ? e0 : gallop_u32(ix.ids, a, e0, tile_hi);
+                    int64_t a = single ? cur[tid] : (t == 0 ? s0 : first_unit(ix, s0, e0, tile_lo));
+                    int64_t b = (tile_hi >= N) ? e0 : gallop_u32(ix.codec ? ix.seg_first : ix.ids, a, e0, tile_hi);
                     st.start[tid] = a;
                     st.inc[tid] = W.inc[it];
                     len = (uint32_t)(b - a);
-                    if (single) cur[tid] = b;
+                    // a compressed segment may straddle tile_hi: the next tile starts at it again
+                    if (single) cur[tid] = (ix.codec && b > a) ? b - 1 : b;
                 }
                 uint32_t tot = 0;
                 uint32_t off = block_excl_scan(len, ss.tmp, &tot);
@@ -549,13 +702,13 @@ __global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Wo
                 __syncthreads();
                 if (tot) any_ids = true;
                 if (SMALL) {
-                    stream_ids(ix.ids, st, (uint32_t)mc, tot, [&](uint32_t id, uint32_t) {
+                    stream_units(ix, st, (uint32_t)mc, tot, tile_lo, tile_hi, [&](uint32_t id, uint32_t) {
                         const uint32_t loc = id - tile_lo;
-                        atomicAdd(&cnt[loc >> 2], 1u << ((loc & 3u) << 3));
+                        if (GG_OK(loc, n_ids, 3)) atomicAdd(&cnt[loc >> 2], 1u << ((loc & 3u) << 3));
                     });
                 } else {
-                    stream_ids(ix.ids, st, (uint32_t)mc, tot, [&](uint32_t id, uint32_t inc) {
-                        atomicAdd(&cnt[id - tile_lo], inc);
+                    stream_units(ix, st, (uint32_t)mc, tot, tile_lo, tile_hi, [&](uint32_t id, uint32_t inc) {
+                        if (GG_OK(id - tile_lo, n_ids, 3)) atomicAdd(&cnt[id - tile_lo], inc);
                     });
                 }
                 __syncthreads();
@@ -566,7 +719,8 @@ __global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Wo
             const uint32_t thr = nS == qi.k ? key_prim(S[qi.k - 1]) : 0u;
             TileSet<SMALL> ts{cnt, n_ids, tile_lo, thr, S, nS};
             const uint32_t nn = select_topk(ts, qi.k, SMALL ? 8 : 32, cand, kCandCap, ss);
-            for (uint32_t i = tid; i < nn; i += blockDim.x) S[i] = cand[i];
+            for (uint32_t i = tid; i < nn; i += blockDim.x)
+                if (GG_OK(i, kMaxK, 10)) S[i] = cand[i];
             if (tid == 0) s_nS = nn;
             __syncthreads();
         }
@@ -644,8 +798,10 @@ int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const T
     if (ev) cudaEventRecord(ev[0], s);
     cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), s);
     const int plan_blocks = (int)((Q.n_queries * 32LL + 255) / 256);
-    k_plan<<<plan_blocks, 256, 0, s>>>(ix, Q, W, t);
-    ++launches;
+    k_plan_items<<<plan_blocks, 256, 0, s>>>(ix, Q, W, t);
+    k_unit_scan<<<1, 1024, 0, s>>>(Q, W);
+    k_plan_units<<<plan_blocks, 256, 0, s>>>(ix, Q, W, t);
+    launches += 3;
     if (ev) cudaEventRecord(ev[1], s);
     // persistent grids: as many CTAs as fit on every SM at once
     auto grid = [&](const void *fn, int threads, size_t smem) {

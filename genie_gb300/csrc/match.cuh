@@ -7,6 +7,9 @@
 namespace gg {
 
 Tuning default_tuning();
+// First out-of-bounds report of a build with -DGG_CHECKED: site, index,
+// bound, block<<32|thread (zeros when nothing was reported or unchecked).
+void read_oob(unsigned long long out[4]);
 size_t sparse_smem_bytes(const Tuning &t, bool packed);
 size_t dense_smem_bytes(const Tuning &t, bool small);
 cudaError_t prepare_kernels(const Tuning &t);

@@ -85,8 +85,14 @@ int save_index(const genie_index *ix, const char *path) {
         ok = dump(ix->d_ids, (size_t)ix->n_ids * 4);
     } else {
         ok = dump(ix->d_words, (size_t)ix->n_words * 4) && dump(ix->d_key_seg, (size_t)(n_keys + 1) * 8) &&
-             dump(ix->d_seg_word_off, (size_t)(ix->n_segs + 1) * 8) && dump(ix->d_seg_first, (size_t)ix->n_segs * 4) &&
-             dump(ix->d_seg_len, (size_t)ix->n_segs * 4);
+             dump(ix->d_seg_word_off, (size_t)(ix->n_segs + 1) * 8) && dump(ix->d_seg_first, (size_t)ix->n_segs * 4);
+        if (ok) {   // the device keeps segment positions; the file keeps lengths
+            std::vector<int64_t> pos((size_t)ix->n_segs + 1);
+            std::vector<uint32_t> len((size_t)ix->n_segs);
+            ok = cudaMemcpy(pos.data(), ix->d_seg_len.p, pos.size() * 8, cudaMemcpyDeviceToHost) == cudaSuccess;
+            for (size_t s = 0; ok && s < len.size(); ++s) len[s] = (uint32_t)(pos[s + 1] - pos[s]);
+            ok = ok && (len.empty() || w.put(len.data(), len.size() * 4));
+        }
     }
     if (!ok) return fail(GENIE_ERR_IO, "write failed: %s", path);
     uint64_t sum = w.h.h;

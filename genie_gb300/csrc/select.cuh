@@ -20,6 +20,8 @@ struct SelectScratch {
     uint32_t hist[256];
     uint32_t sc[16];
     uint32_t tmp[48];
+    unsigned long long tot64;
+    unsigned long long pad;
 };
 
 // Find, in a warp, the digit d (scanning bins from `from_top` order) at which

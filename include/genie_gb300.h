@@ -167,7 +167,7 @@ typedef struct {
     int64_t max_items;
     uint32_t max_k;
     int32_t use_graph;       /* capture the device work as one CUDA graph */
-    int32_t autotune;        /* reserved: tune with genie_batch_autotune */
+    int64_t max_units;       /* (dim,value) lists the items may cover; 0: 16 * max_items */
 } genie_batch_config;
 
 /* Kernel shape knobs picked by the autotuner (0 keeps the current value). */
