@@ -291,6 +291,7 @@ int genie_batch_run(genie_batch *b, const genie_queries *q, uint32_t *out_ids, u
     cudaEventRecord(b->ev0, b->stream);
     rc = enqueue(b, b->stream);
     cudaEventRecord(b->ev1, b->stream);
+    b->launched = rc == GENIE_OK;
     if (rc) return rc;
     rc = fetch_async(b, b->stream, out_scores != nullptr);
     if (rc) return rc;
