@@ -211,7 +211,10 @@ def main():
     n_items = int(batch["item_off"][-1])
     Q = qb.n_queries
 
-    stream = torch.cuda.current_stream()
+    # one non-default stream carries the L2 flushes, the events and the graph
+    # launches (a null handle would select the batch's own stream instead)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")     # > 2x the 129 MB L2
 
     bt = g.Batch(table, Q, n_items, 100, use_graph=True)

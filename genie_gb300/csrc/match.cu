@@ -38,35 +38,47 @@ void read_oob(unsigned long long out[4]) {
 // A range item covers several lists whose concatenation is not sorted, so
 // every later search inside a span happens per unit.
 
-__global__ void __launch_bounds__(256) k_plan_items(DevIndex ix, DevQueries Q, Work W, Tuning T) {
-    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+constexpr int kPlanThreads = 128;
+
+__global__ void __launch_bounds__(kPlanThreads) k_plan_items(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+    __shared__ unsigned long long s_total, s_units;
+    __shared__ unsigned int s_maxw, s_bad;
+    const int64_t q = blockIdx.x;
     const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
     if (q >= nq) return;
-    const uint32_t lane = lane_id();
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
     const int64_t i0 = Q.item_off[q], i1 = Q.item_off[q + 1];
     const int32_t m = (int32_t)(i1 - i0);
     const uint32_t k = Q.k ? Q.k[q] : (Q.dyn ? Q.dyn[1] : Q.uniform_k);
     const bool weighted = Q.weighted && Q.weight && Q.weighted[q];
+    if (tid == 0) {
+        s_total = 0;
+        s_units = 0;
+        s_maxw = 0;
+        s_bad = 0;
+    }
+    __syncthreads();
     int32_t scale = 0;
     if (weighted) {
-        int bad = 0;
-        if (lane == 0) {
-            double s = 0.0;
-            for (int64_t i = i0; i < i1; ++i) {
-                float w = Q.weight[i];
-                if (!(w > 0.0f) || isinf(w)) bad = 1;
-                s += (double)w;
-            }
-            int e = 0;
-            (void)frexp(s, &e);
-            scale = 31 - e;
+        // the scale depends on m * max(w) only, so it is independent of any
+        // summation order: every sum of the item weights stays below 2^31
+        float mx = 0.0f;
+        unsigned bad = 0;
+        for (int64_t i = i0 + tid; i < i1; i += nt) {
+            const float w = Q.weight[i];
+            if (!(w > 0.0f) || isinf(w)) bad = 1;
+            else mx = fmaxf(mx, w);
         }
-        scale = __shfl_sync(0xffffffffu, scale, 0);
-        bad = __shfl_sync(0xffffffffu, bad, 0);
-        if (bad && lane == 0) atomicOr(&W.ctr[kCtrError], kErrWeight);
+        atomicMax(&s_maxw, __float_as_uint(mx));     // positive floats order as their bits
+        if (bad) atomicOr(&s_bad, 1u);
+        __syncthreads();
+        int e = 0;
+        (void)frexp((double)m * (double)__uint_as_float(s_maxw), &e);
+        scale = 31 - e;
+        if (s_bad && tid == 0) atomicOr(&W.ctr[kCtrError], kErrWeight);
     }
-    int64_t total = 0, units = 0;
-    for (int64_t i = i0 + lane; i < i1; i += 32) {
+    uint64_t total = 0, units = 0;
+    for (int64_t i = i0 + tid; i < i1; i += nt) {
         if (!GG_OK(i, W.items_cap, 7)) break;
         int32_t d = Q.dim[i], lo = Q.low[i], hi = Q.up[i];
         int64_t k0 = 0, nk = 0;
@@ -77,23 +89,28 @@ __global__ void __launch_bounds__(256) k_plan_items(DevIndex ix, DevQueries Q, W
                 if (hi > mx) hi = mx;
                 k0 = ix.key_base[d] + ((int64_t)lo - mn);
                 nk = (int64_t)hi - lo + 1;
-                total += ix.key_off[k0 + nk] - ix.key_off[k0];
+                total += (uint64_t)(ix.key_off[k0 + nk] - ix.key_off[k0]);
             }
         }
         W.item_k0[i] = k0;
-        W.item_nk[i] = nk;
+        W.item_nk[i] = (uint32_t)nk;
         uint32_t inc = 1;
         if (weighted) inc = (uint32_t)__double2ll_rn(ldexp((double)Q.weight[i], scale));
         W.item_inc[i] = inc;
-        units += nk;
+        units += (uint64_t)nk;
     }
-    total = (int64_t)warp_sum_u64((uint64_t)total);
-    units = (int64_t)warp_sum_u64((uint64_t)units);
-    if (lane == 0 && GG_OK(q, W.q_cap, 12)) {
+    total = warp_sum_u64(total);
+    units = warp_sum_u64(units);
+    if (lane_id() == 0) {
+        atomicAdd(&s_total, (unsigned long long)total);
+        atomicAdd(&s_units, (unsigned long long)units);
+    }
+    __syncthreads();
+    if (tid == 0 && GG_OK(q, W.q_cap, 12)) {
         QInfo qi;
-        qi.total = total;
+        qi.total = (int64_t)s_total;
         qi.unit0 = 0;
-        qi.n_units = units;
+        qi.n_units = (int32_t)s_units;
         qi.item0 = i0;
         qi.n_items = m;
         qi.k = k;
@@ -101,12 +118,12 @@ __global__ void __launch_bounds__(256) k_plan_items(DevIndex ix, DevQueries Q, W
         qi.flags = weighted ? kFlagWeighted : 0;
         // bound on any object's count: one match per item on a one-value-per-dim
         // table; on a bag table, every covered list may repeat the object
-        const int64_t bound = ix.is_bag ? units * ix.mult_max : (int64_t)m;
+        const int64_t bound = ix.is_bag ? (int64_t)s_units * ix.mult_max : (int64_t)m;
         if (!weighted && bound <= 255) qi.flags |= kFlagSmallCount;
         qi.parts = 1;
         qi.cls = kClsNone;
         W.qinfo[q] = qi;
-        W.q_unit_off[q] = units;
+        W.q_unit_off[q] = (int64_t)s_units;
         W.done[q] = 0;
         W.qstate[q] = 0;
         if (k == 0 || k > (uint32_t)kMaxK) atomicOr(&W.ctr[kCtrError], kErrCapacity);
@@ -141,27 +158,27 @@ __global__ void __launch_bounds__(1024) k_unit_scan(DevQueries Q, Work W) {
     }
 }
 
-__global__ void __launch_bounds__(256) k_plan_units(DevIndex ix, DevQueries Q, Work W, Tuning T) {
-    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void __launch_bounds__(kPlanThreads) k_plan_units(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+    __shared__ uint32_t s_tmp[48];
+    const int64_t q = blockIdx.x;
     const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
     if (q >= nq) return;
-    const uint32_t lane = lane_id();
+    const uint32_t tid = threadIdx.x, nt = blockDim.x;
     QInfo qi = W.qinfo[q];
     const bool fits = W.q_unit_off[nq] <= W.units_cap;
     if (fits) {
         int64_t base = qi.unit0;
         const int64_t i1 = qi.item0 + qi.n_items;
-        for (int64_t c = qi.item0; c < i1; c += 32) {
-            const int64_t i = c + lane;
-            const int64_t nk = i < i1 ? (int64_t)W.item_nk[i] : 0;
-            // units fit 32 bits within one warp step
-            const uint32_t incl = warp_incl_scan((uint32_t)nk);
-            const int64_t u0 = base + incl - nk;
+        for (int64_t c = qi.item0; c < i1; c += nt) {
+            const int64_t i = c + tid;
+            const uint32_t nk = i < i1 ? W.item_nk[i] : 0u;
+            uint32_t tot = 0;
+            const uint32_t ex = block_excl_scan(nk, s_tmp, &tot);
             if (nk) {
                 const int64_t k0 = W.item_k0[i];
                 const uint32_t inc = W.item_inc[i];
-                for (int64_t j = 0; j < nk; ++j) {
-                    const int64_t u = u0 + j, key = k0 + j;
+                for (uint32_t j = 0; j < nk; ++j) {
+                    const int64_t u = base + ex + j, key = k0 + j;
                     if (!GG_OK(u, W.units_cap, 14)) break;
                     const int64_t a = ix.codec ? ix.key_seg[key] : ix.key_off[key];
                     const int64_t e = ix.codec ? ix.key_seg[key + 1] : ix.key_off[key + 1];
@@ -170,10 +187,10 @@ __global__ void __launch_bounds__(256) k_plan_units(DevIndex ix, DevQueries Q, W
                     W.inc[u] = inc;
                 }
             }
-            base += __shfl_sync(0xffffffffu, incl, 31);
+            base += tot;
         }
     }
-    if (lane == 0) {
+    if (tid == 0) {
         const uint32_t k = qi.k;
         const bool small = (qi.flags & kFlagSmallCount) != 0;
         const int64_t total = qi.total;
@@ -209,10 +226,9 @@ __global__ void __launch_bounds__(256) k_plan_units(DevIndex ix, DevQueries Q, W
         }
     }
     // queries without any matching posting: padded results right away
-    __syncwarp();
     if (qi.k >= 1 && qi.k <= (uint32_t)kMaxK && qi.total == 0) {
         const int64_t o = Q.out_off[q];
-        for (uint32_t j = lane; j < qi.k; j += 32) {
+        for (uint32_t j = tid; j < qi.k; j += nt) {
             if (!GG_OK(o + j, W.out_cap, 4)) break;
             W.out_ids[o + j] = 0;
             W.out_counts[o + j] = 0;
@@ -222,6 +238,12 @@ __global__ void __launch_bounds__(256) k_plan_units(DevIndex ix, DevQueries Q, W
 }
 
 // ------------------------------------------------------------------ shared
+
+// Sparse kernel: promoted-slot list placed behind the staged units.
+constexpr int kPromOff = ((kItemChunk * 20 + 4) + 15) / 16 * 16;
+constexpr int kPromCap = 1024;
+static_assert(kPromOff + kPromCap * 4 <= kCandCap * 8, "promoted list must fit the union region");
+static_assert(kPromCap * 8 <= kPromOff, "candidate keys of the promoted list must end below it");
 
 // Items of one query part staged in shared memory.
 struct ItemStage {
@@ -488,7 +510,10 @@ __global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Wo
     st.flat = (uint32_t *)(uni + kItemChunk * 16);
     uint64_t *cand = (uint64_t *)uni;
     SelectScratch &ss = *(SelectScratch *)(uni + kCandCap * 8);
-    __shared__ uint32_t s_work;
+    // slots whose count reached 2, behind the staged units (candidates later
+    // overwrite the units, never this list: kPromCap keys end below it)
+    uint32_t *prom = (uint32_t *)(uni + kPromOff);
+    __shared__ uint32_t s_work, s_prom;
 
     const int list = PACKED ? kListSparsePacked : kListSparseWide;
     for (;;) {
@@ -524,6 +549,7 @@ __global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Wo
             uint4 *t4 = (uint4 *)tab_raw;
             const uint32_t n4 = (cap * (PACKED ? 4 : 8) + 15) / 16;
             for (uint32_t i = tid; i < n4; i += blockDim.x) t4[i] = make_uint4(0, 0, 0, 0);
+            if (tid == 0) s_prom = 0;
             __syncthreads();
             for (int32_t c0 = 0; c0 < qi.n_units; c0 += kItemChunk) {
                 const int32_t mc = min(kItemChunk, qi.n_units - c0);
@@ -544,7 +570,14 @@ __global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Wo
                                 if (old == 0u) return;
                                 cur = old;
                             }
-                            if ((cur >> 8) == id) { atomicAdd(&tab[h], 1u); return; }
+                            if ((cur >> 8) == id) {
+                                // the one increment that takes a slot from 1 to 2 promotes it
+                                if ((atomicAdd(&tab[h], 1u) & 255u) == 1u) {
+                                    const uint32_t at = atomicAdd(&s_prom, 1u);
+                                    if (at < (uint32_t)kPromCap) prom[at] = h;
+                                }
+                                return;
+                            }
                             h = (h + 1 == cap) ? 0 : h + 1;
                         }
                     });
@@ -571,9 +604,27 @@ __global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Wo
                 }
                 __syncthreads();
             }
-            HashSet<PACKED> hs{tab_raw, cap};
-            const int bits = PACKED ? 8 : 32;
-            nres = select_topk(hs, qi.k, bits, cand_out, kCandCap, ss);
+            const uint32_t n_prom = PACKED ? s_prom : 0u;
+            if (PACKED && n_prom >= qi.k && n_prom <= (uint32_t)kPromCap) {
+                // every slot outside the promoted list holds a count of 1, below
+                // every promoted count: the exact top-k lies inside the list
+                const uint32_t *tab = (const uint32_t *)tab_raw;
+                const uint32_t np2 = next_pow2(n_prom);
+                for (uint32_t i = tid; i < np2; i += blockDim.x) {
+                    uint64_t key = 0;
+                    if (i < n_prom) {
+                        const uint32_t v = tab[prom[i]];
+                        key = make_key(v & 255u, v >> 8);
+                    }
+                    cand_out[i] = key;
+                }
+                bitonic_sort_desc(cand_out, np2);
+                nres = qi.k;
+            } else {
+                HashSet<PACKED> hs{tab_raw, cap};
+                const int bits = PACKED ? 8 : 32;
+                nres = select_topk(hs, qi.k, bits, cand_out, kCandCap, ss);
+            }
         }
         finish_part(ix, W, T, Q, q, p, qi, cand_out, nres, ss, overflow);
         __syncthreads();
@@ -797,10 +848,9 @@ int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const T
     int launches = 0;
     if (ev) cudaEventRecord(ev[0], s);
     cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), s);
-    const int plan_blocks = (int)((Q.n_queries * 32LL + 255) / 256);
-    k_plan_items<<<plan_blocks, 256, 0, s>>>(ix, Q, W, t);
+    k_plan_items<<<Q.n_queries, kPlanThreads, 0, s>>>(ix, Q, W, t);
     k_unit_scan<<<1, 1024, 0, s>>>(Q, W);
-    k_plan_units<<<plan_blocks, 256, 0, s>>>(ix, Q, W, t);
+    k_plan_units<<<Q.n_queries, kPlanThreads, 0, s>>>(ix, Q, W, t);
     launches += 3;
     if (ev) cudaEventRecord(ev[1], s);
     // persistent grids: as many CTAs as fit on every SM at once

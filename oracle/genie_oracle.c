@@ -171,10 +171,10 @@ void orc_adaptive_range(const orc_index *ix, int32_t dim, float sel,
 /* ------------------------------------------------------------------ */
 
 int32_t orc_weight_scale(const float *w, int64_t m) {
-    double s = 0.0;
-    for (int64_t i = 0; i < m; ++i) s += (double)w[i];
+    float mx = 0.0f;
+    for (int64_t i = 0; i < m; ++i) mx = w[i] > mx ? w[i] : mx;
     int e = 0;
-    (void)frexp(s, &e);             /* s < 2^e */
+    (void)frexp((double)m * (double)mx, &e);   /* any sum of the weights < m*max < 2^e */
     return 31 - e;
 }
 

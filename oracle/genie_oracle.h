@@ -62,8 +62,9 @@ int  orc_item_span(const orc_index *ix, int32_t dim, int32_t low, int32_t up,
 void orc_adaptive_range(const orc_index *ix, int32_t dim, float sel,
                         int32_t *low, int32_t *up);
 
-/* Fixed-point scale exponent s for a weighted query: weights are summed as
- * llrint(w * 2^s) in 64-bit integers, s = 31 - e where sum(w) < 2^e. */
+/* Fixed-point scale exponent s for a weighted query of m items: weights are
+ * summed as llrint(w * 2^s), s = 31 - e where m * max(w) < 2^e, so every sum
+ * fits 32 bits and the scale does not depend on summation order. */
 int32_t orc_weight_scale(const float *w, int64_t m);
 
 /*
