@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_units(DevIndex ix, DevQue
         if (fits && k >= 1 && k <= (uint32_t)kMaxK && total > 0) {
             const bool packed = small && ix.n_objects <= (int64_t)(1u << 24);
             const int64_t slots = packed ? T.sparse_slots_packed : T.sparse_slots_wide;
-            const int64_t cap = slots * 3 / 4;
+            const int64_t cap = slots / 2;      // load factor <= 1/2
             const int64_t ps = (total + cap - 1) / cap;
             if (total <= T.sparse_max_total && ps <= kMaxParts && total * 4 <= ix.n_objects * 3) {
                 qi.cls = kClsSparse;
@@ -288,9 +288,103 @@ __device__ __forceinline__ void stream_ids(const uint32_t *__restrict__ ids, int
                 }
             }
         }
+        visit(v, inc);
+    }
+}
+
+// Per-id form of stream_ids.
+template <class V>
+__device__ __forceinline__ void stream_ids1(const uint32_t *__restrict__ ids, int64_t n_ids, const ItemStage &st,
+                                            uint32_t n_items, uint32_t F, V &&visit) {
+    stream_ids(ids, n_ids, st, n_items, F, [&](uint32_t(&v)[8], uint32_t(&inc)[8]) {
 #pragma unroll
         for (int j = 0; j < 8; ++j)
             if (inc[j]) visit(v[j], inc[j]);
+    });
+}
+
+// Home slot of an id in a table of `cap` slots (multiplicative hash, then a
+// multiply-high range reduction, so cap need not be a power of two).
+__device__ __forceinline__ uint32_t slot_of(uint32_t id, uint32_t cap) {
+    return (uint32_t)(((uint64_t)(id * 0x9E3779B1u) * cap) >> 32);
+}
+
+// Lane-queue hash insert.  Each lane holds up to 8 ids (inc == 0: no id) and
+// moves on to its next id as soon as the current one is placed, so a warp
+// step costs the longest per-lane sum of probes instead of the sum of the
+// per-id longest probes.  Linear probing, at most `cap` probes per id.
+// PACKED slots are id<<8 | count (ids < 2^24, counts <= 255); the one
+// increment taking a slot from 1 to 2 appends the slot to `prom`.
+// Wide slots are (id+1)<<32 | sum.
+template <bool PACKED>
+__device__ __forceinline__ void hash_insert8(void *tab_raw, uint32_t cap, uint32_t (&v)[8], uint32_t (&inc)[8],
+                                             uint32_t *prom, uint32_t *s_prom) {
+    auto pop = [&]() {
+#pragma unroll
+        for (int t = 0; t < 7; ++t) {
+            v[t] = v[t + 1];
+            inc[t] = inc[t + 1];
+        }
+        v[7] = 0;
+        inc[7] = 0;
+    };
+    int left = 8;
+    while (left > 0 && inc[0] == 0) {
+        pop();
+        --left;
+    }
+    uint32_t h = left ? slot_of(v[0], cap) : 0u, probes = 0;
+    while (__any_sync(0xffffffffu, left > 0)) {
+        if (left <= 0) continue;
+        bool done = false;
+        const uint32_t id = v[0];
+        if (!GG_OK(h, cap, 2)) {
+            done = true;
+        } else if (PACKED) {
+            uint32_t *tab = (uint32_t *)tab_raw;
+            uint32_t cur = tab[h];
+            if (cur == 0u) {
+                const uint32_t old = atomicCAS(&tab[h], 0u, (id << 8) | 1u);
+                if (old == 0u) done = true;
+                else cur = old;
+            }
+            if (!done && (cur >> 8) == id) {
+                if ((atomicAdd(&tab[h], 1u) & 255u) == 1u) {
+                    const uint32_t at = atomicAdd(s_prom, 1u);
+                    if (at < (uint32_t)kPromCap) prom[at] = h;
+                }
+                done = true;
+            }
+        } else {
+            unsigned long long *tab = (unsigned long long *)tab_raw;
+            const unsigned long long tag = (unsigned long long)(id + 1u) << 32;
+            unsigned long long cur = tab[h];
+            if (cur == 0ull) {
+                const unsigned long long old = atomicCAS(&tab[h], 0ull, tag | inc[0]);
+                if (old == 0ull) done = true;
+                else cur = old;
+            }
+            if (!done && (cur & 0xFFFFFFFF00000000ull) == tag) {
+                atomicAdd(&tab[h], (unsigned long long)inc[0]);
+                done = true;
+            }
+        }
+        if (!done) {
+            h = (h + 1 == cap) ? 0u : h + 1;
+            if (++probes >= cap) done = true;
+        }
+        if (done) {
+            pop();
+            --left;
+            while (left > 0 && inc[0] == 0) {
+                pop();
+                --left;
+            }
+            if (left > 0) {
+                h = slot_of(v[0], cap);
+                probes = 0;
+            }
+        }
     }
 }
 
@@ -320,7 +414,7 @@ template <class V>
 __device__ __forceinline__ void stream_units(const DevIndex &ix, const ItemStage &st, uint32_t n_items, uint32_t F,
                                              uint32_t lo, uint32_t hi, V &&visit) {
     if (ix.codec) stream_segments(ix, st, n_items, F, lo, hi, visit);
-    else stream_ids(ix.ids, ix.n_ids, st, n_items, F, visit);
+    else stream_ids1(ix.ids, ix.n_ids, st, n_items, F, visit);
 }
 
 // First unit (posting position, or segment of a compressed index) of the
@@ -463,9 +557,6 @@ __device__ void finish_part(const DevIndex &ix, const Work &W, const Tuning &T, 
 
 // ------------------------------------------------------------------ sparse
 
-__device__ __forceinline__ uint32_t slot_of(uint32_t id, uint32_t cap) {
-    return (uint32_t)(((uint64_t)(id * 0x9E3779B1u) * cap) >> 32);
-}
 
 template <bool PACKED>
 struct HashSet {
@@ -538,11 +629,11 @@ __global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Wo
             if (qi.n_units > kItemChunk) __syncthreads();
         }
         const bool single = qi.n_units <= kItemChunk;
-        const bool overflow = part_total > (uint64_t)slots_max * 3 / 4;
+        const bool overflow = part_total > (uint64_t)slots_max / 2;
         uint64_t *cand_out = cand;
         uint32_t nres = 0;
         if (!overflow) {
-            uint32_t cap = (uint32_t)umin64((uint64_t)slots_max, part_total + part_total / 3 + 64);
+            uint32_t cap = (uint32_t)umin64((uint64_t)slots_max, 2 * part_total + 64);
             cap = (cap + 31) & ~31u;
             if (cap > slots_max) cap = slots_max;
             // zero the table
@@ -557,7 +648,14 @@ __global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Wo
                     stage_range(ix, W, qi, c0, mc, P > 1 && p > 0, P > 1 && p < P - 1, id_lo, id_hi, st, ss);
                 __syncthreads();
                 const uint32_t F = st.flat[mc];
-                if (PACKED) {
+                if (!ix.codec) {
+                    // plain lists: 8 ids per lane, lane-queue insert
+                    stream_ids(ix.ids, ix.n_ids, st, (uint32_t)mc, F, [&](uint32_t(&v)[8], uint32_t(&inc)[8]) {
+                        hash_insert8<PACKED>(tab_raw, cap, v, inc, prom, &s_prom);
+                    });
+                } else if (PACKED) {
+                    // compressed lists: ids arrive one by one from the warp decoders
+                    // (divergent lanes), so every lane probes on its own
                     uint32_t *tab = (uint32_t *)tab_raw;
                     stream_units(ix, st, (uint32_t)mc, F, id_lo, id_hi, [&](uint32_t id, uint32_t) {
                         uint32_t h = slot_of(id, cap);
