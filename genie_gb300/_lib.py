@@ -52,6 +52,7 @@ PROTOTYPES = {
     "genie_index_load": (ctypes.c_int, [ctypes.c_char_p, P]),
     "genie_search": (ctypes.c_int, [P, P, P, P, P]),
     "genie_search_multi": (ctypes.c_int, [P, P, I32, P, P, P]),
+    "genie_search_noalloc": (ctypes.c_int, [P, P, P, I64, I64, P, P, P, P]),
     "genie_batch_create": (ctypes.c_int, [P, P, P]),
     "genie_batch_destroy": (ctypes.c_int, [P]),
     "genie_batch_run": (ctypes.c_int, [P, P, P, P, P]),

@@ -160,6 +160,25 @@ int genie_search(genie_index *ix, const genie_queries *q, uint32_t *out_ids,
 int genie_search_multi(genie_index *const *ix, const genie_queries *q, int32_t n_index,
                        uint32_t *out_ids, uint32_t *out_counts, float *out_scores);
 
+/* Search that allocates no memory, for callers that may not call cudaMalloc:
+ * a host framework or server that owns every device allocation, or a caller
+ * with a hard memory budget or a latency-critical path (cudaMalloc/cudaFree
+ * synchronise the device).  No counterpart in the reference: this entry
+ * point is this library's own.  All pointers in q, out_off and the outputs
+ * are DEVICE pointers (q->n_queries and q->uniform_k are host values);
+ * n_items = item_off[n_queries], total_k = sum of k.  The workspace is a
+ * fixed 16 MiB device array inside the library, shared by every call: at
+ * most 1024 queries, 262144 items, 262144 covered (dim,value) lists and
+ * 32768 results per call, larger batches are rejected with
+ * GENIE_ERR_INVALID_ARG.  The first call on a device looks up the array's
+ * address (and prepares the kernels); make it before any stream capture.
+ * Calls are serialised and wait for their device work on `stream` (a
+ * cudaStream_t, NULL = legacy default); device work that overlaps a call
+ * from elsewhere in the process would race on the shared array. */
+int genie_search_noalloc(genie_index *ix, const genie_queries *q, const int64_t *out_off,
+                         int64_t n_items, int64_t total_k, uint32_t *out_ids, uint32_t *out_counts,
+                         float *out_scores, void *stream);
+
 /* ---------------------------------------------------------------- batched */
 
 typedef struct {
