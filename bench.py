@@ -51,6 +51,8 @@ def parse():
     p.add_argument("--queries", type=int, default=1024)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-autotune", action="store_true")
+    p.add_argument("--tuning", default="",
+                   help="fixed kernel shape, e.g. sparse_slots=53248,sparse_ctas_per_sm=1 (skips autotuning)")
     return p.parse_args()
 
 
@@ -218,7 +220,11 @@ def main():
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")     # > 2x the 129 MB L2
 
     bt = g.Batch(table, Q, n_items, 100, use_graph=True)
-    tuning = bt.tuning() if args.no_autotune else bt.autotune(qb)
+    if args.tuning:
+        bt.set_tuning(**{kv.split("=")[0]: int(kv.split("=")[1]) for kv in args.tuning.split(",")})
+        tuning = bt.tuning()
+    else:
+        tuning = bt.tuning() if args.no_autotune else bt.autotune(qb)
     bt.stage(qb)
 
     # ---- value: device-resident batch, graph launches, L2 flushed per step

@@ -184,7 +184,11 @@ Tuning from_public(const Tuning &base, const genie_tuning &t) {
         r.sparse_slots_packed = (t.sparse_slots + 31) & ~31;
         r.sparse_slots_wide = ((t.sparse_slots / 2) + 31) & ~31;
     }
-    if (t.sparse_ctas_per_sm > 0) r.sparse_ctas_per_sm = t.sparse_ctas_per_sm;
+    if (t.sparse_ctas_per_sm > 0) {
+        r.sparse_ctas_per_sm = t.sparse_ctas_per_sm == 1 ? 1 : 2;
+        r.sparse_threads = t.sparse_ctas_per_sm == 1 ? 1024 : 512;
+    }
+    if (t.sparse_load_pct > 0) r.sparse_load_pct = t.sparse_load_pct;
     if (t.dense_tile > 0) {
         r.dense_tile_u8 = (t.dense_tile + 255) & ~255;
         r.dense_tile_u32 = ((t.dense_tile / 4) + 63) & ~63;
@@ -202,6 +206,8 @@ void to_public(const Tuning &r, genie_tuning &t) {
     t.dense_threads = r.dense_threads;
     t.sparse_max_total = r.sparse_max_total;
     t.dense_part_work = r.dense_part_work;
+    t.sparse_load_pct = r.sparse_load_pct;
+    t.reserved = 0;
 }
 
 }  // namespace
@@ -307,10 +313,12 @@ int genie_batch_get_tuning(const genie_batch *b, genie_tuning *out) {
 int genie_batch_set_tuning(genie_batch *b, const genie_tuning *t) {
     if (!b || !t) return fail(GENIE_ERR_INVALID_ARG, "NULL argument");
     Tuning r = from_public(b->tuning, *t);
-    if (r.sparse_slots_packed < 1024 || sparse_smem_bytes(r, true) > 227 * 1024 ||
-        sparse_smem_bytes(r, false) > 227 * 1024 || r.dense_tile_u8 < 4096 ||
-        dense_smem_bytes(r, true) > 227 * 1024 || dense_smem_bytes(r, false) > 227 * 1024 ||
-        (r.dense_threads != 512 && r.dense_threads != 1024))
+    const size_t smem_cap = 227 * 1024 - 64;     // dynamic + the kernels' static words
+    if (r.sparse_slots_packed < 1024 || sparse_smem_bytes(r, true) > smem_cap ||
+        sparse_smem_bytes(r, false) > smem_cap || r.dense_tile_u8 < 4096 ||
+        dense_smem_bytes(r, true) > smem_cap || dense_smem_bytes(r, false) > smem_cap ||
+        (r.dense_threads != 512 && r.dense_threads != 1024) || r.sparse_load_pct < 25 ||
+        r.sparse_load_pct > 90)
         return fail(GENIE_ERR_INVALID_ARG, "tuning outside the supported shapes");
     b->tuning = r;
     b->graph_valid = false;
@@ -351,17 +359,20 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
     int rc = genie_batch_stage(b, sample);
     if (rc) return rc;
     const Tuning base = b->tuning;
-    struct Cand { int32_t slots, tile; int64_t smax; };
+    // hash slots, CTAs per SM (2: 512 threads, 1: 1024 threads), load %, dense tile, crossover
+    struct Cand { int32_t slots, ctas, load, tile; int64_t smax; };
     const Cand cands[] = {
-        {22528, 147456, 16 * 16896}, {11264, 147456, 16 * 16896}, {33792, 147456, 16 * 16896},
-        {22528, 98304, 16 * 16896}, {22528, 196608, 16 * 16896}, {22528, 147456, 4 * 16896},
-        {22528, 147456, 64 * 16896},
+        {22528, 2, 50, 147456, 270336}, {11264, 2, 50, 147456, 270336}, {22528, 2, 60, 147456, 270336},
+        {45056, 1, 50, 147456, 270336}, {53248, 1, 56, 147456, 270336}, {53248, 1, 62, 147456, 270336},
+        {22528, 2, 50, 98304, 270336},  {22528, 2, 50, 147456, 67584},  {53248, 1, 62, 147456, 1081344},
     };
     float best_ms = 1e30f;
     Tuning best = base;
     for (const Cand &c : cands) {
         genie_tuning t{};
         t.sparse_slots = c.slots;
+        t.sparse_ctas_per_sm = c.ctas;
+        t.sparse_load_pct = c.load;
         t.dense_tile = c.tile;
         t.sparse_max_total = c.smax;
         if (genie_batch_set_tuning(b, &t)) continue;

@@ -87,6 +87,7 @@ struct Tuning {
     int64_t dense_part_work;       // touched ids per dense part
     int32_t sparse_ctas_per_sm;
     int32_t dense_ctas_per_sm;
+    int32_t sparse_load_pct;       // posting ids per part <= this % of the hash slots
 };
 
 // Work lists, one per kernel variant.

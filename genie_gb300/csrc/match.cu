@@ -198,7 +198,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_units(DevIndex ix, DevQue
         if (fits && k >= 1 && k <= (uint32_t)kMaxK && total > 0) {
             const bool packed = small && ix.n_objects <= (int64_t)(1u << 24);
             const int64_t slots = packed ? T.sparse_slots_packed : T.sparse_slots_wide;
-            const int64_t cap = slots / 2;      // load factor <= 1/2
+            const int64_t cap = slots * T.sparse_load_pct / 100;     // table load factor bound
             const int64_t ps = (total + cap - 1) / cap;
             if (total <= T.sparse_max_total && ps <= kMaxParts && total * 4 <= ix.n_objects * 3) {
                 qi.cls = kClsSparse;
@@ -586,8 +586,10 @@ struct HashSet {
 
 // Per-part hash of object id -> count (or fixed-point weight sum) in shared
 // memory; replaces the per-query bitmap + c-PQ (match_device_utils.h:160-446).
-template <bool PACKED>
-__global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+// NT = 512: two CTAs per SM with mid-size tables; NT = 1024: one CTA per SM
+// with the largest table, so a query needs fewer id-range parts.
+template <bool PACKED, int NT>
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_sparse(DevIndex ix, DevQueries Q, Work W, Tuning T) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t tid = threadIdx.x;
     const uint32_t slots_max = PACKED ? (uint32_t)T.sparse_slots_packed : (uint32_t)T.sparse_slots_wide;
@@ -629,11 +631,11 @@ __global__ void __launch_bounds__(512, 2) k_sparse(DevIndex ix, DevQueries Q, Wo
             if (qi.n_units > kItemChunk) __syncthreads();
         }
         const bool single = qi.n_units <= kItemChunk;
-        const bool overflow = part_total > (uint64_t)slots_max / 2;
+        const bool overflow = part_total * 100 > (uint64_t)slots_max * T.sparse_load_pct;
         uint64_t *cand_out = cand;
         uint32_t nres = 0;
         if (!overflow) {
-            uint32_t cap = (uint32_t)umin64((uint64_t)slots_max, 2 * part_total + 64);
+            uint32_t cap = (uint32_t)umin64((uint64_t)slots_max, part_total * 100 / T.sparse_load_pct + 64);
             cap = (cap + 31) & ~31u;
             if (cap > slots_max) cap = slots_max;
             // zero the table
@@ -907,6 +909,7 @@ Tuning default_tuning() {
     t.dense_part_work = 4 << 20;
     t.sparse_ctas_per_sm = 2;
     t.dense_ctas_per_sm = 1;
+    t.sparse_load_pct = 50;
     return t;
 }
 
@@ -916,8 +919,10 @@ static cudaError_t set_smem(const void *fn, size_t bytes) {
 
 cudaError_t prepare_kernels(const Tuning &t) {
     cudaError_t e;
-    if ((e = set_smem((const void *)k_sparse<true>, sparse_smem_bytes(t, true)))) return e;
-    if ((e = set_smem((const void *)k_sparse<false>, sparse_smem_bytes(t, false)))) return e;
+    if ((e = set_smem((const void *)k_sparse<true, 512>, sparse_smem_bytes(t, true)))) return e;
+    if ((e = set_smem((const void *)k_sparse<false, 512>, sparse_smem_bytes(t, false)))) return e;
+    if ((e = set_smem((const void *)k_sparse<true, 1024>, sparse_smem_bytes(t, true)))) return e;
+    if ((e = set_smem((const void *)k_sparse<false, 1024>, sparse_smem_bytes(t, false)))) return e;
     if ((e = set_smem((const void *)k_dense<true>, dense_smem_bytes(t, true)))) return e;
     if ((e = set_smem((const void *)k_dense<false>, dense_smem_bytes(t, false)))) return e;
     return cudaSuccess;
@@ -928,7 +933,8 @@ cudaError_t prepare_kernels_max() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (optin <= 0) optin = 227 * 1024;
-    const void *fns[] = {(const void *)k_sparse<true>, (const void *)k_sparse<false>,
+    const void *fns[] = {(const void *)k_sparse<true, 512>, (const void *)k_sparse<false, 512>,
+                         (const void *)k_sparse<true, 1024>, (const void *)k_sparse<false, 1024>,
                          (const void *)k_dense<true>, (const void *)k_dense<false>};
     for (const void *fn : fns) {
         cudaFuncAttributes a;
@@ -959,9 +965,15 @@ int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const T
     };
     const size_t sp = sparse_smem_bytes(t, true), sw = sparse_smem_bytes(t, false);
     const size_t dp = dense_smem_bytes(t, true), dw = dense_smem_bytes(t, false);
-    k_sparse<true><<<grid((const void *)k_sparse<true>, t.sparse_threads, sp), t.sparse_threads, sp, s>>>(ix, Q, W, t);
-    if (ev) cudaEventRecord(ev[2], s);
-    k_sparse<false><<<grid((const void *)k_sparse<false>, t.sparse_threads, sw), t.sparse_threads, sw, s>>>(ix, Q, W, t);
+    if (t.sparse_threads == 1024) {
+        k_sparse<true, 1024><<<grid((const void *)k_sparse<true, 1024>, 1024, sp), 1024, sp, s>>>(ix, Q, W, t);
+        if (ev) cudaEventRecord(ev[2], s);
+        k_sparse<false, 1024><<<grid((const void *)k_sparse<false, 1024>, 1024, sw), 1024, sw, s>>>(ix, Q, W, t);
+    } else {
+        k_sparse<true, 512><<<grid((const void *)k_sparse<true, 512>, 512, sp), 512, sp, s>>>(ix, Q, W, t);
+        if (ev) cudaEventRecord(ev[2], s);
+        k_sparse<false, 512><<<grid((const void *)k_sparse<false, 512>, 512, sw), 512, sw, s>>>(ix, Q, W, t);
+    }
     if (ev) cudaEventRecord(ev[3], s);
     k_dense<true><<<grid((const void *)k_dense<true>, t.dense_threads, dp), t.dense_threads, dp, s>>>(ix, Q, W, t);
     if (ev) cudaEventRecord(ev[4], s);

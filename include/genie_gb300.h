@@ -192,11 +192,13 @@ typedef struct {
 /* Kernel shape knobs picked by the autotuner (0 keeps the current value). */
 typedef struct {
     int32_t sparse_slots;       /* hash slots per CTA (4-byte slots; 8-byte get half) */
-    int32_t sparse_ctas_per_sm;
+    int32_t sparse_ctas_per_sm; /* 2: 512-thread CTAs, 1: 1024-thread CTAs */
     int32_t dense_tile;         /* ids per dense tile (1-byte counters; 4-byte get a quarter) */
     int32_t dense_threads;
     int64_t sparse_max_total;   /* queries touching more posting ids go dense */
     int64_t dense_part_work;    /* posting ids per dense id-range part */
+    int32_t sparse_load_pct;    /* posting ids per part <= this % of the hash slots */
+    int32_t reserved;
 } genie_tuning;
 
 /* Batched search over one resident index: fixed-capacity device buffers,

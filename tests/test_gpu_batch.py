@@ -72,6 +72,24 @@ def test_autotune_keeps_results_exact(genie, oracle):
     bt.set_tuning(sparse_slots=4096, dense_tile=16384)
     ids2, cnt2 = bt.run(qb)
     assert np.array_equal(ids2, oid) and np.array_equal(cnt2, ocnt)
+    # one 1024-thread CTA per SM with the largest table and a higher load
+    bt.set_tuning(sparse_slots=53248, sparse_ctas_per_sm=1, sparse_load_pct=62, dense_tile=147456)
+    ids3, cnt3 = bt.run(qb)
+    assert np.array_equal(ids3, oid) and np.array_equal(cnt3, ocnt)
+    with pytest.raises(genie.cpu_runtime_error):
+        bt.set_tuning(sparse_load_pct=95)
+
+
+def test_big_table_variant_on_lsh_batch(genie, oracle):
+    from genie_gb300 import workloads
+    values, batch = workloads.config1(n=300_000, q=48, k=100)
+    t = genie.Table.from_values(values)
+    qb = _qb(genie, batch)
+    bt = genie.Batch(t, 48, int(batch["item_off"][-1]), 100)
+    bt.set_tuning(sparse_slots=53248, sparse_ctas_per_sm=1, sparse_load_pct=62)
+    ids, cnt = bt.run(qb)
+    oid, ocnt, _, _ = oracle.Index(values).search(qb.as_oracle_batch())
+    assert np.array_equal(ids, oid) and np.array_equal(cnt, ocnt)
 
 
 def test_batch_capacity_errors(genie):
