@@ -108,6 +108,15 @@ class Clocks:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def count(self):
+        return len(self.lines)
+
+    def wait_samples(self, n, work, limit_s=5.0):
+        """Run `work` (untimed launches of the same batch) until n samples exist."""
+        t0 = time.time()
+        while self.proc and self.count() < n and time.time() - t0 < limit_s:
+            work()
+
     def stop(self):
         if not self.proc:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
@@ -232,8 +241,18 @@ def main():
         flush.zero_()
         bt.launch(stream.cuda_stream)
     torch.cuda.synchronize()
+
+    def load():     # untimed steps of the same batch, so that clock samples see the GPU under load
+        for _ in range(64):
+            flush.zero_()
+            bt.launch(stream.cuda_stream)
+        torch.cuda.synchronize()
+
+    # the timed region lasts milliseconds, below nvidia-smi's 200 ms sampling
+    # period: samples are taken over untimed steps right before and after it
     clocks = Clocks(local)
     clocks.start()
+    clocks.wait_samples(2, load)
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
@@ -245,23 +264,26 @@ def main():
         e.record(stream)
     torch.cuda.synchronize()
     step_ms = [s.elapsed_time(e) for s, e in evs]
+    clocks.wait_samples(clocks.count() + 2, load)
     clock_info = clocks.stop()
+    clock_info["window"] = "200 ms samples over untimed steps of the same batch around the timed region"
     total_ms = max_over_ranks(sum(step_ms), dist, True)
     value = world * Q * args.steps / (total_ms / 1e3)
     ids_graph, cnt_graph = bt.fetch()
+    kernels_per_step = bt.last_stats()[0]
 
     # ---- roofline: per-kernel events (direct launches, same tuning and flushing)
     bp = g.Batch(table, Q, n_items, 100, use_graph=False)
     bp.set_tuning(**{k: v for k, v in tuning.items()})
     bp.stage(qb)
-    stage_tot = np.zeros(5)
+    stage_tot = np.zeros(6)
     for i in range(args.warmup + args.steps):
         flush.zero_()
         bp.launch(stream.cuda_stream)
         ms = bp.stage_ms()
         if i >= args.warmup:
             stage_tot += ms
-    names = ["k_plan", "k_sparse<packed>", "k_sparse<wide>", "k_dense<u8>", "k_dense<u32>"]
+    names = ["k_plan", "k_bitmap", "k_sparse<packed>", "k_sparse<wide>", "k_dense<u8>", "k_dense<u32>"]
     dom = int(np.argmax(stage_tot[1:]) + 1)
     dom_ms = stage_tot[dom] / args.steps
     peak, peak_kind = peaks()
@@ -329,12 +351,12 @@ def main():
                        "l2": "flushed by a 512 MiB device write before every timed step",
                        "tuning": tuning, "parallelism": "replica per GPU" if world > 1 else "single GPU"},
             "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "plain_e2e": {"value": plain, "unit": "queries/s", "path": "genie_search (per-call upload, 5 launches)",
+            "plain_e2e": {"value": plain, "unit": "queries/s", "path": "genie_search (per-call upload and launch)",
                           "batched_over_plain": e2e / plain, "same_results": same},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "clocks": clock_info,
-            "gpu_launches": 5 * args.steps,
+            "gpu_launches": kernels_per_step * args.steps,
         }
         print(json.dumps(line))
     if dist is not None:

@@ -196,6 +196,8 @@ Tuning from_public(const Tuning &base, const genie_tuning &t) {
     if (t.dense_threads > 0) r.dense_threads = t.dense_threads;
     if (t.sparse_max_total > 0) r.sparse_max_total = t.sparse_max_total;
     if (t.dense_part_work > 0) r.dense_part_work = t.dense_part_work;
+    if (t.bitmap_bits > 0) r.bitmap_bits = (t.bitmap_bits + 31) & ~31;
+    if (t.bitmap_bits < 0) r.bitmap_bits = 0;
     return r;
 }
 
@@ -207,7 +209,7 @@ void to_public(const Tuning &r, genie_tuning &t) {
     t.sparse_max_total = r.sparse_max_total;
     t.dense_part_work = r.dense_part_work;
     t.sparse_load_pct = r.sparse_load_pct;
-    t.reserved = 0;
+    t.bitmap_bits = r.bitmap_bits > 0 ? r.bitmap_bits : -1;
 }
 
 }  // namespace
@@ -318,7 +320,7 @@ int genie_batch_set_tuning(genie_batch *b, const genie_tuning *t) {
         sparse_smem_bytes(r, false) > smem_cap || r.dense_tile_u8 < 4096 ||
         dense_smem_bytes(r, true) > smem_cap || dense_smem_bytes(r, false) > smem_cap ||
         (r.dense_threads != 512 && r.dense_threads != 1024) || r.sparse_load_pct < 25 ||
-        r.sparse_load_pct > 90)
+        r.sparse_load_pct > 90 || (r.bitmap_bits > 0 && (r.bitmap_bits < 8192 || bitmap_smem_bytes(r) > smem_cap)))
         return fail(GENIE_ERR_INVALID_ARG, "tuning outside the supported shapes");
     b->tuning = r;
     b->graph_valid = false;
@@ -352,19 +354,25 @@ int genie_batch_stage_ms(const genie_batch *b, float *ms) {
 
 // Times each candidate shape on the sample (one warm-up, three timed graph
 // launches) and keeps the fastest.  Candidates vary the hash slots per CTA
-// (hence CTAs per SM), the dense tile and the sparse/dense crossover.
+// (hence CTAs per SM), the dense tile, the sparse/dense crossover and the
+// presence-bitmap kernel (on with a bitmap size, or off).
 int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuning *chosen) {
     if (!b || !sample) return fail(GENIE_ERR_INVALID_ARG, "NULL argument");
     cudaSetDevice(b->ix->device);
     int rc = genie_batch_stage(b, sample);
     if (rc) return rc;
     const Tuning base = b->tuning;
-    // hash slots, CTAs per SM (2: 512 threads, 1: 1024 threads), load %, dense tile, crossover
-    struct Cand { int32_t slots, ctas, load, tile; int64_t smax; };
+    // hash slots, CTAs per SM (2: 512 threads, 1: 1024 threads), load %, dense tile,
+    // crossover, presence bits per bitmap CTA (-1: bitmap kernel off)
+    struct Cand { int32_t slots, ctas, load, tile; int64_t smax; int32_t bits; };
     const Cand cands[] = {
-        {22528, 2, 50, 147456, 270336}, {11264, 2, 50, 147456, 270336}, {22528, 2, 60, 147456, 270336},
-        {45056, 1, 50, 147456, 270336}, {53248, 1, 56, 147456, 270336}, {53248, 1, 62, 147456, 270336},
-        {22528, 2, 50, 98304, 270336},  {22528, 2, 50, 147456, 67584},  {53248, 1, 62, 147456, 1081344},
+        {22528, 2, 50, 147456, 270336, -1}, {11264, 2, 50, 147456, 270336, -1},
+        {22528, 2, 60, 147456, 270336, -1}, {45056, 1, 50, 147456, 270336, -1},
+        {53248, 1, 56, 147456, 270336, -1}, {53248, 1, 62, 147456, 270336, -1},
+        {22528, 2, 50, 98304, 270336, -1},  {22528, 2, 50, 147456, 67584, -1},
+        {53248, 1, 62, 147456, 1081344, -1},
+        {53248, 1, 56, 147456, 270336, 1310720}, {53248, 1, 56, 147456, 1081344, 1310720},
+        {22528, 2, 50, 147456, 270336, 655360},  {53248, 1, 56, 147456, 270336, 524288},
     };
     float best_ms = 1e30f;
     Tuning best = base;
@@ -375,6 +383,7 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
         t.sparse_load_pct = c.load;
         t.dense_tile = c.tile;
         t.sparse_max_total = c.smax;
+        t.bitmap_bits = c.bits;
         if (genie_batch_set_tuning(b, &t)) continue;
         float total = 0.0f;
         bool ok = true;

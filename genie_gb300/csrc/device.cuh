@@ -88,11 +88,13 @@ struct Tuning {
     int32_t sparse_ctas_per_sm;
     int32_t dense_ctas_per_sm;
     int32_t sparse_load_pct;       // posting ids per part <= this % of the hash slots
+    int32_t bitmap_bits;           // presence bits per k_bitmap CTA (0: bitmap path off)
+    int32_t bitmap_multi_slots;    // slots of its table of ids seen twice or more
 };
 
 // Work lists, one per kernel variant.
 enum : int { kListSparsePacked = 0, kListSparseWide = 1, kListDenseSmall = 2, kListDenseWide = 3,
-             kNumLists = 4 };
+             kListBitmap = 4, kNumLists = 5 };
 constexpr int kCtrError = 2 * kNumLists;     // ctr[2c] = items in list c, ctr[2c+1] = next
 constexpr int kCtrWords = 2 * kNumLists + 2;
 

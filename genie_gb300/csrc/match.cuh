@@ -18,10 +18,11 @@ cudaError_t prepare_kernels_max();
 
 // Enqueue plan + sparse + dense kernels for one batch on stream s.  All
 // pointers in Q and W are device pointers; W arrays are sized for Q.
-// Returns the number of kernel launches issued.  With `ev` (6 events), event
-// i+1 is recorded after stage i: plan, sparse-packed, sparse-wide,
+// Returns the number of kernel launches issued.  With `ev` (7 events), event
+// i+1 is recorded after stage i: plan, bitmap, sparse-packed, sparse-wide,
 // dense-small, dense-wide (event 0 before the plan).
-constexpr int kStages = 5;
+constexpr int kStages = 6;
+size_t bitmap_smem_bytes(const Tuning &t);
 int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t,
                  int num_sms, cudaStream_t s, cudaEvent_t *ev = nullptr);
 

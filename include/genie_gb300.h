@@ -198,7 +198,7 @@ typedef struct {
     int64_t sparse_max_total;   /* queries touching more posting ids go dense */
     int64_t dense_part_work;    /* posting ids per dense id-range part */
     int32_t sparse_load_pct;    /* posting ids per part <= this % of the hash slots */
-    int32_t reserved;
+    int32_t bitmap_bits;        /* presence bits per bitmap CTA; -1 turns the bitmap kernel off */
 } genie_tuning;
 
 /* Batched search over one resident index: fixed-capacity device buffers,
@@ -226,9 +226,9 @@ int genie_batch_set_tuning(genie_batch *b, const genie_tuning *t);
  * (between events around the device work; waits for it to finish). */
 int genie_batch_last_stats(const genie_batch *b, int32_t *kernels, float *device_ms);
 /* Device milliseconds of each stage of the last launch of a batch created
- * with use_graph = 0: ms[0] plan (+ counter reset), ms[1] sparse 4-byte-slot
- * kernel, ms[2] sparse 8-byte-slot kernel, ms[3] dense 1-byte-counter kernel,
- * ms[4] dense 4-byte-counter kernel. */
+ * with use_graph = 0: ms[0] plan (+ counter reset), ms[1] presence-bitmap
+ * kernel, ms[2] sparse 4-byte-slot kernel, ms[3] sparse 8-byte-slot kernel,
+ * ms[4] dense 1-byte-counter kernel, ms[5] dense 4-byte-counter kernel. */
 int genie_batch_stage_ms(const genie_batch *b, float *ms);
 
 /* ---------------------------------------------------------------- codecs */
