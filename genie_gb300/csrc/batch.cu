@@ -196,7 +196,7 @@ Tuning from_public(const Tuning &base, const genie_tuning &t) {
     if (t.dense_threads > 0) r.dense_threads = t.dense_threads;
     if (t.sparse_max_total > 0) r.sparse_max_total = t.sparse_max_total;
     if (t.dense_part_work > 0) r.dense_part_work = t.dense_part_work;
-    if (t.bitmap_bits > 0) r.bitmap_bits = (t.bitmap_bits + 31) & ~31;
+    if (t.bitmap_bits > 0) r.bitmap_bits = t.bitmap_bits;
     if (t.bitmap_bits < 0) r.bitmap_bits = 0;
     return r;
 }
@@ -320,7 +320,7 @@ int genie_batch_set_tuning(genie_batch *b, const genie_tuning *t) {
         sparse_smem_bytes(r, false) > smem_cap || r.dense_tile_u8 < 4096 ||
         dense_smem_bytes(r, true) > smem_cap || dense_smem_bytes(r, false) > smem_cap ||
         (r.dense_threads != 512 && r.dense_threads != 1024) || r.sparse_load_pct < 25 ||
-        r.sparse_load_pct > 90 || (r.bitmap_bits > 0 && (r.bitmap_bits < 8192 || bitmap_smem_bytes(r) > smem_cap)))
+        r.sparse_load_pct > 90 || (r.bitmap_bits > 0 && (r.bitmap_bits < 8192 || r.bitmap_bits > (1 << 24))))
         return fail(GENIE_ERR_INVALID_ARG, "tuning outside the supported shapes");
     b->tuning = r;
     b->graph_valid = false;
@@ -363,7 +363,7 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
     if (rc) return rc;
     const Tuning base = b->tuning;
     // hash slots, CTAs per SM (2: 512 threads, 1: 1024 threads), load %, dense tile,
-    // crossover, presence bits per bitmap CTA (-1: bitmap kernel off)
+    // crossover, largest id space of the bitmap kernel (-1: bitmap kernel off)
     struct Cand { int32_t slots, ctas, load, tile; int64_t smax; int32_t bits; };
     const Cand cands[] = {
         {22528, 2, 50, 147456, 270336, -1}, {11264, 2, 50, 147456, 270336, -1},
@@ -371,8 +371,8 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
         {53248, 1, 56, 147456, 270336, -1}, {53248, 1, 62, 147456, 270336, -1},
         {22528, 2, 50, 98304, 270336, -1},  {22528, 2, 50, 147456, 67584, -1},
         {53248, 1, 62, 147456, 1081344, -1},
-        {53248, 1, 56, 147456, 270336, 1310720}, {53248, 1, 56, 147456, 1081344, 1310720},
-        {22528, 2, 50, 147456, 270336, 655360},  {53248, 1, 56, 147456, 270336, 524288},
+        {53248, 1, 56, 147456, 270336, 1179648}, {53248, 1, 56, 147456, 1081344, 1179648},
+        {22528, 2, 50, 147456, 270336, 1179648},
     };
     float best_ms = 1e30f;
     Tuning best = base;

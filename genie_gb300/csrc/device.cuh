@@ -23,7 +23,10 @@ constexpr int kCandCap = 2048;       // candidate buffer of the top-k selection
 
 enum : uint8_t { kClsNone = 0, kClsSparse = 1, kClsDense = 2 };
 enum : uint8_t { kFlagWeighted = 1, kFlagSmallCount = 2, kFlagRetry = 4, kFlagPacked = 8 };
-enum : uint32_t { kErrWeight = 1, kErrOverflow = 2, kErrCapacity = 4, kErrUnits = 8 };
+// posting lists a query may cover on the bitmap path (its span buffers)
+constexpr uint32_t kBmSpanCap = 256;
+
+enum : uint32_t { kErrWeight = 1, kErrOverflow = 2, kErrCapacity = 4, kErrUnits = 8, kErrTimeout = 16 };
 
 struct DevIndex {
     const uint32_t *ids;
@@ -88,8 +91,9 @@ struct Tuning {
     int32_t sparse_ctas_per_sm;
     int32_t dense_ctas_per_sm;
     int32_t sparse_load_pct;       // posting ids per part <= this % of the hash slots
-    int32_t bitmap_bits;           // presence bits per k_bitmap CTA (0: bitmap path off)
+    int32_t bitmap_bits;           // largest id space of the bitmap kernel (0: off)
     int32_t bitmap_multi_slots;    // slots of its table of ids seen twice or more
+    int32_t bitmap_pages;          // its ring pages (set per launch from the id space)
 };
 
 // Work lists, one per kernel variant.
@@ -227,13 +231,105 @@ __device__ __forceinline__ uint64_t make_key(uint32_t prim, uint32_t id) {
 __device__ __forceinline__ uint32_t key_prim(uint64_t k) { return (uint32_t)(k >> 32); }
 __device__ __forceinline__ uint32_t key_id(uint64_t k) { return 0xFFFFFFFFu - (uint32_t)k; }
 
-// Descending bitonic sort of n (power of two) keys in shared memory.
+// A group of threads that cooperates like a block: the whole block, or the
+// warps [1, 1 + N/32) of a warp-specialized block, synchronized by named
+// barrier 1 (the first warp runs on its own).
+struct BlockGroup {
+    __device__ static uint32_t rank() { return threadIdx.x; }
+    __device__ static uint32_t size() { return blockDim.x; }
+    __device__ static void sync() { __syncthreads(); }
+};
+template <uint32_t N>
+struct TailGroup {
+    __device__ static uint32_t rank() { return threadIdx.x - 32u; }
+    __device__ static uint32_t size() { return N; }
+    __device__ static void sync() { asm volatile("bar.sync 1, %0;" ::"n"(N) : "memory"); }
+};
+
+// Compare-exchange: the larger key when keep_max, else the smaller.
+__device__ __forceinline__ uint64_t cmpx(uint64_t x, uint64_t y, bool keep_max) {
+    return (keep_max == (x > y)) ? x : y;
+}
+
+// Bitonic stages of one merge size with strides <= 32 on two keys per thread
+// (x0 = key 2t, x1 = key 2t+1): the partner of a stride >= 2 lives in lane
+// t ^ (stride/2) of the same warp, so no shared memory or barrier is needed.
+// Every lane of the warp must take part.
+__device__ __forceinline__ void bitonic_reg_stages(uint64_t &x0, uint64_t &x1, uint32_t t, uint32_t size,
+                                                   uint32_t stride) {
+    const bool desc = ((2u * t) & size) == 0;
+    for (; stride >= 2; stride >>= 1) {
+        const uint32_t d = stride >> 1;
+        const bool lower = ((2u * t) & stride) == 0;
+        const uint64_t y0 = __shfl_xor_sync(0xffffffffu, x0, d);
+        const uint64_t y1 = __shfl_xor_sync(0xffffffffu, x1, d);
+        x0 = cmpx(x0, y0, lower == desc);
+        x1 = cmpx(x1, y1, lower == desc);
+    }
+    const uint64_t hi = x0 > x1 ? x0 : x1, lo = x0 > x1 ? x1 : x0;
+    x0 = desc ? hi : lo;
+    x1 = desc ? lo : hi;
+}
+
+// Descending bitonic sort of n (power of two) keys in shared memory.  Strides
+// up to 32 run in registers (shuffles); only the longer strides of the merges
+// of 128 keys and more go through shared memory, one barrier each.
+template <class G = BlockGroup>
 __device__ __forceinline__ void bitonic_sort_desc(uint64_t *a, uint32_t n) {
+    const uint32_t t = G::rank(), nt = G::size();
+    G::sync();
+    if (n <= 1) return;
+    if (n <= 64) {          // one warp, keys past n read as 0 (the smallest key)
+        if (t < 32) {
+            uint64_t x0 = 2 * t < n ? a[2 * t] : 0ull, x1 = 2 * t + 1 < n ? a[2 * t + 1] : 0ull;
+            for (uint32_t size = 2; size <= 64; size <<= 1) bitonic_reg_stages(x0, x1, t, size, size >> 1);
+            if (2 * t < n) a[2 * t] = x0;
+            if (2 * t + 1 < n) a[2 * t + 1] = x1;
+        }
+        G::sync();
+        return;
+    }
+    if (n <= 2 * nt) {
+        const bool act = t < n / 2;      // whole warps: n/2 is a multiple of 32
+        uint64_t x0 = 0, x1 = 0;
+        if (act) {
+            x0 = a[2 * t];
+            x1 = a[2 * t + 1];
+            for (uint32_t size = 2; size <= 64; size <<= 1) bitonic_reg_stages(x0, x1, t, size, size >> 1);
+        }
+        for (uint32_t size = 128; size <= n; size <<= 1) {
+            if (act) {
+                a[2 * t] = x0;
+                a[2 * t + 1] = x1;
+            }
+            for (uint32_t stride = size >> 1; stride >= 64; stride >>= 1) {
+                G::sync();
+                if (act) {
+                    const uint32_t i = 2 * t - (t & (stride - 1)), j = i + stride;
+                    const bool desc = (i & size) == 0;
+                    const uint64_t x = a[i], y = a[j];
+                    if ((x < y) == desc) { a[i] = y; a[j] = x; }
+                }
+            }
+            G::sync();
+            if (act) {
+                x0 = a[2 * t];
+                x1 = a[2 * t + 1];
+                bitonic_reg_stages(x0, x1, t, size, 32);
+            }
+        }
+        if (act) {
+            a[2 * t] = x0;
+            a[2 * t + 1] = x1;
+        }
+        G::sync();
+        return;
+    }
     for (uint32_t size = 2; size <= n; size <<= 1) {
         for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-            __syncthreads();
-            for (uint32_t t = threadIdx.x; t < n / 2; t += blockDim.x) {
-                uint32_t i = 2 * t - (t & (stride - 1));
+            G::sync();
+            for (uint32_t u = t; u < n / 2; u += nt) {
+                uint32_t i = 2 * u - (u & (stride - 1));
                 uint32_t j = i + stride;
                 bool desc = ((i & size) == 0);
                 uint64_t x = a[i], y = a[j];
@@ -241,7 +337,7 @@ __device__ __forceinline__ void bitonic_sort_desc(uint64_t *a, uint32_t n) {
             }
         }
     }
-    __syncthreads();
+    G::sync();
 }
 
 __device__ __forceinline__ uint32_t next_pow2(uint32_t v) {

@@ -201,12 +201,12 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_units(DevIndex ix, DevQue
             const int64_t slots = packed ? T.sparse_slots_packed : T.sparse_slots_wide;
             const int64_t cap = slots * T.sparse_load_pct / 100;     // table load factor bound
             const int64_t ps = (total + cap - 1) / cap;
-            const int64_t pb = T.bitmap_bits > 0 ? (ix.n_objects + T.bitmap_bits - 1) / T.bitmap_bits : 0;
-            if (total <= T.sparse_max_total && total * 4 <= ix.n_objects * 3 && packed && pb >= 1 &&
-                pb <= kMaxParts && !ix.codec) {
-                // presence bitmap over an id range + a table of repeated ids
+            if (total <= T.sparse_max_total && total * 4 <= ix.n_objects * 3 && packed && !ix.codec &&
+                T.bitmap_bits > 0 && T.bitmap_pages >= 2 && ix.n_objects <= T.bitmap_bits &&
+                qi.n_units <= (int32_t)kBmSpanCap) {
+                // presence bitmap over the whole id space + a table of repeated ids
                 qi.cls = kClsSparse;
-                qi.parts = (uint16_t)pb;
+                qi.parts = 1;
                 qi.flags |= kFlagPacked;
                 list = kListBitmap;
             } else if (total <= T.sparse_max_total && ps <= kMaxParts && total * 4 <= ix.n_objects * 3) {
@@ -742,180 +742,11 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_sparse(DevIndex ix, D
 
 // ------------------------------------------------------------------ bitmap
 
-// Warp-per-unit streaming: a warp walks U sorted lists at a time, 4 ids per
-// lane per list and step (coalesced), so no lane searches for its unit and
-// every lane keeps 4*U loads in flight.
-template <int U, class V>
-__device__ __forceinline__ void stream_units_by_warp(const uint32_t *__restrict__ ids, const ItemStage &st,
-                                                     uint32_t n_units, V &&visit) {
-    const uint32_t lane = lane_id(), nw = blockDim.x >> 5;
-    for (uint32_t u0 = warp_id(); u0 < n_units; u0 += nw * U) {
-        int64_t s[U];
-        uint32_t len[U], inc[U], most = 0;
-#pragma unroll
-        for (int j = 0; j < U; ++j) {
-            const uint32_t u = u0 + j * nw;
-            const bool ok = u < n_units;
-            s[j] = ok ? st.start[u] : 0;
-            len[j] = ok ? st.len[u] : 0u;
-            inc[j] = ok ? st.inc[u] : 0u;
-            most = max(most, len[j]);
-        }
-        for (uint32_t b = 0; b < most; b += 128) {
-            uint32_t v[U][4];
-#pragma unroll
-            for (int j = 0; j < U; ++j)
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const uint32_t x = b + i * 32 + lane;
-                    v[j][i] = x < len[j] ? __ldg(ids + s[j] + x) : 0u;
-                }
-#pragma unroll
-            for (int j = 0; j < U; ++j)
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    if (b + i * 32 + lane < len[j]) visit(v[j][i], inc[j]);
-        }
-    }
-}
+}  // namespace gg
 
-// Presence bitmap over the part's id range plus a small table of the ids seen
-// twice or more.  A first occurrence is one atomicOr on a bit -- no probing --
-// and only repeated ids reach the table (slot = id<<8 | count, count >= 2).
-// If the table holds >= k ids, the top-k lies among them (every other id has
-// count 1); otherwise it is the whole table plus the smallest ids whose bit is
-// set and that are not in the table.  Reference counterpart: the bitmap count
-// plus c-PQ of match_AT (match_device_utils.h:160-446).
-__global__ void __launch_bounds__(1024, 1) k_bitmap(DevIndex ix, DevQueries Q, Work W, Tuning T) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    const uint32_t bm_words = ((uint32_t)T.bitmap_bits + 31) / 32;
-    const uint32_t mslots = (uint32_t)T.bitmap_multi_slots;
-    uint32_t *bm = (uint32_t *)smem;
-    uint32_t *mt = bm + ((bm_words + 3) & ~3u);
-    unsigned char *uni = (unsigned char *)(mt + mslots);
-    ItemStage st;
-    st.start = (int64_t *)uni;
-    st.len = (uint32_t *)(uni + kItemChunk * 8);
-    st.inc = (uint32_t *)(uni + kItemChunk * 12);
-    st.flat = (uint32_t *)(uni + kItemChunk * 16);
-    uint64_t *cand = (uint64_t *)uni;
-    SelectScratch &ss = *(SelectScratch *)(uni + kCandCap * 8);
-    __shared__ uint32_t s_work, s_multi, s_ovf, s_n;
+#include "bitmap.cuh"
 
-    for (;;) {
-        if (tid == 0) s_work = atomicAdd(&W.ctr[2 * kListBitmap + 1], 1u);
-        __syncthreads();
-        const uint32_t w = s_work;
-        __syncthreads();
-        if (w >= *(volatile uint32_t *)&W.ctr[2 * kListBitmap]) break;
-        const uint2 wk = W.work[(size_t)kListBitmap * W.work_stride + w];
-        const uint32_t q = wk.x, p = wk.y;
-        if (!GG_OK(q, W.q_cap, 12)) continue;
-        const QInfo qi = W.qinfo[q];
-        const uint32_t P = qi.parts;
-        const uint32_t lo = (uint32_t)(((uint64_t)ix.n_objects * p) / P);
-        const uint32_t hi = (uint32_t)(((uint64_t)ix.n_objects * (p + 1)) / P);
-        const uint32_t words = (hi - lo + 31) / 32;
-        // clear the bitmap words of this range and the table
-        for (uint32_t i = tid; i < (words + 3) / 4; i += nt) ((uint4 *)bm)[i] = make_uint4(0u, 0u, 0u, 0u);
-        for (uint32_t i = tid; i < mslots / 4; i += nt) ((uint4 *)mt)[i] = make_uint4(0u, 0u, 0u, 0u);
-        if (tid == 0) {
-            s_multi = 0;
-            s_ovf = 0;
-        }
-        const uint32_t mcap = mslots / 2;     // table load factor <= 1/2
-        for (int32_t c0 = 0; c0 < qi.n_units; c0 += kItemChunk) {
-            const int32_t mc = min(kItemChunk, qi.n_units - c0);
-            stage_range(ix, W, qi, c0, mc, P > 1 && p > 0, P > 1 && p < P - 1, lo, hi, st, ss);
-            __syncthreads();
-            stream_units_by_warp<4>(ix.ids, st, (uint32_t)mc, [&](uint32_t id, uint32_t) {
-                const uint32_t bit = id - lo;
-                if (!GG_OK(bit >> 5, words, 15)) return;
-                const uint32_t m = 1u << (bit & 31);
-                if (!(atomicOr(&bm[bit >> 5], m) & m)) return;      // first occurrence
-                // seen before: count it in the table of repeated ids
-                uint32_t h = slot_of(id, mslots);
-                for (uint32_t probe = 0; probe < mslots; ++probe) {
-                    uint32_t cur = mt[h];
-                    if (cur == 0u) {
-                        const uint32_t old = atomicCAS(&mt[h], 0u, (id << 8) | 2u);
-                        if (old == 0u) {
-                            if (atomicAdd(&s_multi, 1u) >= mcap) s_ovf = 1;
-                            return;
-                        }
-                        cur = old;
-                    }
-                    if ((cur >> 8) == id) {
-                        atomicAdd(&mt[h], 1u);
-                        return;
-                    }
-                    h = (h + 1 == mslots) ? 0u : h + 1;
-                    if (s_ovf) return;
-                }
-            });
-            __syncthreads();
-        }
-        const bool failed = s_ovf != 0;
-        uint32_t nres = 0;
-        if (!failed) {
-            const uint32_t n_multi = s_multi;
-            if (n_multi >= qi.k) {
-                HashSet<true> hs{mt, mslots};
-                nres = select_topk(hs, qi.k, 8, cand, kCandCap, ss);
-            } else {
-                // the table goes whole; drop its ids from the bitmap, then take the
-                // r smallest remaining ids (count 1) in id order
-                for (uint32_t i = tid; i < mslots; i += nt) {
-                    const uint32_t v = mt[i];
-                    if (v) {
-                        const uint32_t bit = (v >> 8) - lo;
-                        atomicAnd(&bm[bit >> 5], ~(1u << (bit & 31)));
-                    }
-                }
-                if (tid == 0) s_n = 0;
-                __syncthreads();
-                for (uint32_t i = tid; i < mslots; i += nt) {
-                    const uint32_t v = mt[i];
-                    if (v) cand[atomicAdd(&s_n, 1u)] = make_key(v & 255u, v >> 8);
-                }
-                const uint32_t r = qi.k - n_multi;
-                const uint32_t per = (words + nt - 1) / nt;
-                const uint32_t w0 = min(words, tid * per), w1 = min(words, w0 + per);
-                uint32_t c = 0;
-                for (uint32_t i = w0; i < w1; ++i) c += __popc(bm[i]);
-                uint32_t tot = 0;
-                const uint32_t before = block_excl_scan(c, ss.tmp, &tot);
-                if (before < r) {
-                    uint32_t at = before;
-                    for (uint32_t i = w0; i < w1 && at < r; ++i) {
-                        uint32_t x = bm[i];
-                        while (x && at < r) {
-                            const uint32_t b = __ffs(x) - 1;
-                            x &= x - 1;
-                            cand[n_multi + at] = make_key(1u, lo + i * 32 + b);
-                            ++at;
-                        }
-                    }
-                }
-                __syncthreads();
-                const uint32_t n = n_multi + min(r, tot);
-                const uint32_t np2 = next_pow2(n);
-                for (uint32_t i = n + tid; i < np2; i += nt) cand[i] = 0ull;
-                bitonic_sort_desc(cand, np2);
-                nres = min(n, qi.k);
-            }
-        }
-        finish_part(ix, W, T, Q, q, p, qi, cand, nres, ss, failed);
-        __syncthreads();
-    }
-}
-
-size_t bitmap_smem_bytes(const Tuning &t) {
-    const size_t words = ((size_t)t.bitmap_bits + 31) / 32;
-    return ((words + 3) & ~(size_t)3) * 4 + (size_t)t.bitmap_multi_slots * 4 +
-           std::max<size_t>(kItemChunk * 20 + 16, kCandCap * 8) + sizeof(SelectScratch) + 64;
-}
+namespace gg {
 
 // ------------------------------------------------------------------ dense
 
@@ -1096,8 +927,9 @@ Tuning default_tuning() {
     t.sparse_ctas_per_sm = 2;
     t.dense_ctas_per_sm = 1;
     t.sparse_load_pct = 50;
-    t.bitmap_bits = 1310720;         // 160 KiB presence bitmap: one CTA per SM
-    t.bitmap_multi_slots = 8192;     // 32 KiB table of repeated ids
+    t.bitmap_bits = 1179648;         // id spaces up to 144 KiB of presence bits
+    t.bitmap_multi_slots = 4096;     // 16 KiB table of repeated ids
+    t.bitmap_pages = 0;              // set per launch
     return t;
 }
 
@@ -1113,7 +945,6 @@ cudaError_t prepare_kernels(const Tuning &t) {
     if ((e = set_smem((const void *)k_sparse<false, 1024>, sparse_smem_bytes(t, false)))) return e;
     if ((e = set_smem((const void *)k_dense<true>, dense_smem_bytes(t, true)))) return e;
     if ((e = set_smem((const void *)k_dense<false>, dense_smem_bytes(t, false)))) return e;
-    if ((e = set_smem((const void *)k_bitmap, bitmap_smem_bytes(t)))) return e;
     return cudaSuccess;
 }
 
@@ -1135,9 +966,32 @@ cudaError_t prepare_kernels_max() {
     return cudaSuccess;
 }
 
-int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t,
+// Ring pages of the bitmap kernel for an id space of n objects (0: the
+// bitmap, the table and two pages do not fit in shared memory).
+int bitmap_pages(const Tuning &t, int64_t n_objects) {
+    static size_t limit = 0;
+    if (!limit) {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (optin <= 0) optin = 227 * 1024;
+        cudaFuncAttributes a;
+        size_t st = 1024;
+        if (cudaFuncGetAttributes(&a, (const void *)k_bitmap) == cudaSuccess) st = a.sharedSizeBytes;
+        limit = (size_t)optin - st;
+    }
+    if (t.bitmap_bits <= 0 || n_objects > t.bitmap_bits || t.bitmap_multi_slots <= 0) return 0;
+    for (int p = (int)kBmMaxPages; p >= 2; --p)
+        if (bm_layout(n_objects, (uint32_t)t.bitmap_multi_slots, (uint32_t)p).bytes <= limit) return p;
+    return 0;
+}
+
+int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &tun,
                  int num_sms, cudaStream_t s, cudaEvent_t *ev) {
     if (Q.n_queries <= 0) return 0;
+    Tuning t = tun;
+    t.bitmap_pages = bitmap_pages(t, ix.n_objects);
+    if (t.bitmap_pages < 2) t.bitmap_bits = 0;
     int launches = 0;
     if (ev) cudaEventRecord(ev[0], s);
     cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), s);
@@ -1154,8 +1008,10 @@ int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const T
     };
     const size_t sp = sparse_smem_bytes(t, true), sw = sparse_smem_bytes(t, false);
     const size_t dp = dense_smem_bytes(t, true), dw = dense_smem_bytes(t, false);
-    const size_t bp = bitmap_smem_bytes(t);
-    if (t.bitmap_bits > 0) k_bitmap<<<grid((const void *)k_bitmap, 1024, bp), 1024, bp, s>>>(ix, Q, W, t);
+    if (t.bitmap_bits > 0) {
+        const size_t bp = bm_layout(ix.n_objects, (uint32_t)t.bitmap_multi_slots, (uint32_t)t.bitmap_pages).bytes;
+        k_bitmap<<<num_sms, kBmThreads, bp, s>>>(ix, Q, W, t);
+    }
     if (ev) cudaEventRecord(ev[2], s);
     if (t.sparse_threads == 1024) {
         k_sparse<true, 1024><<<grid((const void *)k_sparse<true, 1024>, 1024, sp), 1024, sp, s>>>(ix, Q, W, t);

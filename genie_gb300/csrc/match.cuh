@@ -22,7 +22,8 @@ cudaError_t prepare_kernels_max();
 // i+1 is recorded after stage i: plan, bitmap, sparse-packed, sparse-wide,
 // dense-small, dense-wide (event 0 before the plan).
 constexpr int kStages = 6;
-size_t bitmap_smem_bytes(const Tuning &t);
+// Ring pages of the bitmap kernel for an id space of n objects (0: path off).
+int bitmap_pages(const Tuning &t, int64_t n_objects);
 int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t,
                  int num_sms, cudaStream_t s, cudaEvent_t *ev = nullptr);
 

@@ -198,7 +198,7 @@ typedef struct {
     int64_t sparse_max_total;   /* queries touching more posting ids go dense */
     int64_t dense_part_work;    /* posting ids per dense id-range part */
     int32_t sparse_load_pct;    /* posting ids per part <= this % of the hash slots */
-    int32_t bitmap_bits;        /* presence bits per bitmap CTA; -1 turns the bitmap kernel off */
+    int32_t bitmap_bits;        /* largest id space (objects) of the bitmap kernel; -1: off */
 } genie_tuning;
 
 /* Batched search over one resident index: fixed-capacity device buffers,

@@ -94,16 +94,16 @@ def test_big_table_variant_on_lsh_batch(genie, oracle):
 
 @pytest.mark.parametrize("n", [100_000, 300_000, 1_000_000])
 def test_bitmap_kernel_modes(genie, oracle, n):
-    """The presence-bitmap kernel (one and several id-range parts, the table of
-    repeated ids holding fewer or more than k ids) and the hash kernel give
-    the oracle's answer."""
+    """The presence-bitmap kernel (the table of repeated ids holding fewer or
+    more than k ids), the hash kernel when the id space exceeds the bitmap
+    limit, and the bitmap kernel switched off give the oracle's answer."""
     from genie_gb300 import workloads
     values, batch = workloads.config1(n=n, q=32, k=100)
     t = genie.Table.from_values(values)
     qb = _qb(genie, batch)
     oid, ocnt, _, _ = oracle.Index(values).search(qb.as_oracle_batch())
     bt = genie.Batch(t, 32, int(batch["item_off"][-1]), 100)
-    for bits in (1310720, 65536, 8192, -1):
+    for bits in (1179648, 8192, -1):
         bt.set_tuning(bitmap_bits=bits)
         assert bt.tuning()["bitmap_bits"] == bits
         ids, cnt = bt.run(qb)
