@@ -1,5 +1,5 @@
 // bitmap.cuh -- k_bitmap: match counting of unweighted sparse queries with a
-// presence bitmap over the whole id space, fed by bulk asynchronous copies.
+// presence bitmap over the whole id space.
 //
 // Reference counterpart: the per-query bitmap counter plus c-PQ of match_AT
 // (matching/match_device_utils.h:160-446, match.cu:43-464).  The reference
@@ -7,118 +7,51 @@
 // global atomicCAS per posting id; here one CTA per SM owns an n-bit bitmap in
 // shared memory and a small table of the ids seen twice or more.
 //
-// Warp specialization, one CTA per SM, queries assigned round-robin:
-//   warp 0 (producer)   streams each query's posting lists into a ring of
-//                       shared-memory pages with cp.async.bulk (16-byte
-//                       aligned pieces; the alignment padding is masked out),
-//                       one page per mbarrier phase, running ahead across
-//                       queries so the next query's ids load while the
-//                       consumers select;
-//   warps 1..31         take each page: a first occurrence of an id is one
-//   (consumers)         atomicOr on its bit; a repeat goes to the table
-//                       (id<<8 | count, count >= 2), which also keeps a
-//                       histogram of its counts.  After the last page of a
-//                       query they select its exact top-k and clear the state.
-// Selection: with >= k table ids, the histogram gives the k-th count c*; the
-// ids above c* and the ids at c* are sorted apart (ties by ascending id) and
-// the result is the first k.  With fewer, the result is the whole table, then
-// the smallest ids whose bit is set and that are not in the table (count 1).
-// A full table (overflow) hands the query to the dense kernel.
+// One CTA per SM, queries assigned round-robin, per query:
+//   stage   one 32-id chunk entry per 32 posting ids of every covered list
+//           (the lists' spans were loaded into registers during the previous
+//           query);
+//   stream  warp w takes chunks w, w+32, ...: 16 coalesced chunk loads in
+//           flight per lane, then 16 independent atomicOr on the bitmap; a
+//           first occurrence sets the id's bit, a repeat goes to the table
+//           (id<<8 | count, count >= 2), which also keeps a histogram of its
+//           counts;
+//   select  with >= k table ids, the histogram gives the k-th count c*; the
+//           ids above c* and those at c* are sorted apart (ties by ascending
+//           id) and the result is the first k.  With fewer, the result is the
+//           whole table, then the smallest ids whose bit is set and that are
+//           not in the table (count 1).  A full table hands the query to the
+//           dense kernel;
+//   clear   bitmap, table and histogram.
+// Posting lists are ~100-500 byte runs at random places of the id array:
+// plain loads with many in flight per lane keep more bytes in flight per SM
+// than per-list asynchronous copies.
 #pragma once
 
 namespace gg {
 
 constexpr uint32_t kBmThreads = 1024;
-constexpr uint32_t kBmConsumers = kBmThreads - 32;
-using BmConsumers = TailGroup<kBmConsumers>;
-constexpr uint32_t kBmPageIds = 2048;     // ids per ring page (8 KiB)
-constexpr uint32_t kBmMaxPages = 8;
+constexpr uint32_t kBmChunks = 4096;      // 32-id chunks per query on this path
 constexpr uint32_t kBmProbe = 128;        // longest probe run of the repeated-id table
-constexpr uint32_t kBmSpanSlot = ((kBmSpanCap + 4) * 16 + (kBmSpanCap + 4) * 4 + 127) / 128 * 128;
-constexpr unsigned long long kBmWaitNs = 2000000000ull;   // bound of every wait
-
-struct BmPageHdr {
-    uint32_t q, k, fill, last;
-    int64_t out_off;
-    uint32_t pad[2];
-};
+constexpr int kBmRound = 16;              // chunk loads in flight per lane
 
 // Byte offsets of the shared-memory regions (host and device agree).
 struct BmLayout {
-    uint32_t bm, mt, ring, hdr, mask, span, cand, ss, bar, bytes, bm_words;
+    uint32_t bm, mt, cstart, ccnt, ss, bytes, bm_words;
 };
 __host__ __device__ inline uint32_t bm_align(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
-__host__ __device__ inline BmLayout bm_layout(int64_t n_objects, uint32_t mslots, uint32_t pages) {
+__host__ __device__ inline BmLayout bm_layout(int64_t n_objects, uint32_t mslots) {
     BmLayout L;
     uint32_t o = 0;
     L.bm_words = (uint32_t)((n_objects + 127) / 128) * 4;
-    L.bm = o;   o += bm_align(L.bm_words * 4, 128);
-    L.mt = o;   o += bm_align(mslots * 4, 128);
-    L.ring = o; o += pages * kBmPageIds * 4;
-    L.hdr = o;  o += pages * (uint32_t)sizeof(BmPageHdr);
-    L.mask = o; o += pages * (kBmPageIds / 32) * 4;
-    L.span = o; o += 2 * kBmSpanSlot;
-    L.cand = o; o += kCandCap * 8;
-    L.ss = o;   o += bm_align((uint32_t)sizeof(SelectScratch), 16);
-    L.bar = o;  o += (2 * pages + 2) * 8;
+    L.bm = o;     o += bm_align(L.bm_words * 4, 128);
+    L.mt = o;     o += bm_align(mslots * 4, 128);
+    L.cstart = o; o += kBmChunks * 8;      // also the candidate keys after streaming
+    L.ccnt = o;   o += kBmChunks;
+    L.ss = o;     o += bm_align((uint32_t)sizeof(SelectScratch), 16);
     L.bytes = bm_align(o, 128);
     return L;
 }
-
-// ------------------------------------------------------------ async copies
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
-    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.release.cta.shared::cta.b64 st, [%0];\n\t}" ::"r"(
-                     smem_addr(b))
-                 : "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *b, uint32_t bytes) {
-    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.release.cta.shared::cta.b64 st, [%0], %1;\n\t}" ::
-                     "r"(smem_addr(b)),
-                 "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(b)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-// Wait for the phase of parity `parity` to complete; false after limit_ns.
-__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, unsigned long long limit_ns = kBmWaitNs) {
-    if (mbar_try_wait(b, parity)) return true;
-    const unsigned long long t0 = global_ns();
-    for (;;) {
-        if (mbar_try_wait(b, parity)) return true;
-        if (global_ns() - t0 > limit_ns) return false;
-    }
-}
-// Global -> shared bulk copy (16-byte aligned ends) completing on mbarrier b.
-__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *b) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_addr(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_addr(b))
-                 : "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 
 // ------------------------------------------------------------ selection helpers
 
@@ -187,242 +120,137 @@ __device__ __forceinline__ void warp_append(bool keep, uint64_t key, uint64_t *d
 
 // ------------------------------------------------------------ kernel
 
+struct BmQuery {
+    uint32_t q, k, n_units, pad;
+    int64_t unit0, out_off;
+};
+
 __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQueries Q, Work W, Tuning T) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const uint32_t P = (uint32_t)T.bitmap_pages;
     const uint32_t mslots = (uint32_t)T.bitmap_multi_slots;
-    const BmLayout L = bm_layout(ix.n_objects, mslots, P);
+    const BmLayout L = bm_layout(ix.n_objects, mslots);
     uint32_t *bm = (uint32_t *)(smem + L.bm);
     uint32_t *mt = (uint32_t *)(smem + L.mt);
-    uint32_t *ring = (uint32_t *)(smem + L.ring);
-    BmPageHdr *hdr = (BmPageHdr *)(smem + L.hdr);
-    uint32_t *mask = (uint32_t *)(smem + L.mask);
-    unsigned char *span = smem + L.span;
-    uint64_t *cand = (uint64_t *)(smem + L.cand);
+    int64_t *cstart = (int64_t *)(smem + L.cstart);
+    uint8_t *ccnt = smem + L.ccnt;
+    uint64_t *cand = (uint64_t *)(smem + L.cstart);
     SelectScratch &ss = *(SelectScratch *)(smem + L.ss);
-    uint64_t *full = (uint64_t *)(smem + L.bar), *empty = full + P, *span_full = empty + P;
-    __shared__ uint32_t s_multi, s_ovf, s_n, s_t, s_abort;
+    uint32_t *hist = ss.hist;
+    __shared__ uint32_t s_multi, s_ovf, s_n, s_t;
     __shared__ uint32_t s_spare[32];
+    __shared__ BmQuery s_qd[2];
 
-    const uint32_t tid = threadIdx.x, lane = lane_id();
+    const uint32_t tid = threadIdx.x, lane = lane_id(), warp = warp_id();
     const uint32_t G = gridDim.x, n_work = W.ctr[2 * kListBitmap];
     if (blockIdx.x >= n_work) return;
     const uint2 *work = W.work + (size_t)kListBitmap * W.work_stride;
-    if (tid == 0) {
-        for (uint32_t i = 0; i < P; ++i) {
-            mbar_init(&full[i], 1);
-            mbar_init(&empty[i], kBmConsumers / 32);
-        }
-        mbar_init(&span_full[0], 1);
-        mbar_init(&span_full[1], 1);
-        fence_mbar_init();
-        s_abort = 0;
-        s_multi = 0;
-        s_ovf = 0;
-    }
-    __syncthreads();
-
-    if (tid < 32) {
-        // ---------------------------------------------------------- producer
-        struct QD {
-            uint32_t q, k, n_units;
-            int64_t unit0, out_off;
-        };
-        auto load_qd = [&](uint32_t i) {
-            QD d{};
-            const uint32_t w = blockIdx.x + i * G;
-            if (w < n_work && GG_OK(w, W.work_stride, 16)) {
-                d.q = work[w].x;
-                if (GG_OK(d.q, W.q_cap, 16)) {
-                    const QInfo qi = W.qinfo[d.q];
-                    d.k = qi.k;
-                    d.n_units = (uint32_t)qi.n_units;
-                    d.unit0 = qi.unit0;
-                    d.out_off = Q.out_off[d.q];
-                }
-            }
-            return d;
-        };
-        auto issue_span = [&](uint32_t slot, const QD &d) {     // lane 0
-            fence_proxy_async();
-            unsigned char *sp = span + slot * kBmSpanSlot;
-            const int64_t a0 = d.unit0 & ~(int64_t)1, a1 = (d.unit0 + d.n_units + 1) & ~(int64_t)1;
-            const uint32_t bytes = (uint32_t)(a1 - a0) * 8;
-            mbar_arrive_expect_tx(&span_full[slot], 2 * bytes);
-            bulk_load(sp, W.span_start + a0, bytes, &span_full[slot]);
-            bulk_load(sp + (kBmSpanCap + 4) * 8, W.span_len + a0, bytes, &span_full[slot]);
-        };
-        QD cur{}, nxt{};
-        if (lane == 0) {
-            cur = load_qd(0);
-            issue_span(0, cur);
-            nxt = load_qd(1);
-        }
-        uint32_t pg = 0;
-        bool abort = false;
-        for (uint32_t i = 0; blockIdx.x + i * G < n_work && !abort; ++i) {
-            const uint32_t slot = i & 1;
-            QD after{};
-            if (lane == 0) {
-                if (blockIdx.x + (i + 1) * G < n_work) issue_span(slot ^ 1, nxt);
-                after = load_qd(i + 2);
-                if (!mbar_wait(&span_full[slot], (i >> 1) & 1)) abort = true;
-            }
-            abort = __shfl_sync(0xffffffffu, abort ? 1u : 0u, 0) != 0;
-            if (abort) break;
-            const uint32_t n_units = __shfl_sync(0xffffffffu, cur.n_units, 0);
-            const uint32_t sh = __shfl_sync(0xffffffffu, (uint32_t)(cur.unit0 & 1), 0);
-            const int64_t *sstart = (const int64_t *)(span + slot * kBmSpanSlot) + sh;
-            const int64_t *slen = (const int64_t *)(span + slot * kBmSpanSlot + (kBmSpanCap + 4) * 8) + sh;
-            uint32_t *F = (uint32_t *)(span + slot * kBmSpanSlot + (kBmSpanCap + 4) * 16);
-            // flat offsets of the 16-byte aligned copies of every list
-            uint32_t ftot = 0;
-            for (uint32_t j0 = 0; j0 < n_units; j0 += 32) {
-                const uint32_t j = j0 + lane;
-                uint32_t m = 0;
-                if (j < n_units) {
-                    const int64_t s = sstart[j], e = s + slen[j];
-                    m = (uint32_t)(((e + 3) & ~(int64_t)3) - (s & ~(int64_t)3));
-                }
-                const uint32_t incl = warp_incl_scan(m);
-                if (j < n_units) F[j] = ftot + incl - m;
-                ftot += __shfl_sync(0xffffffffu, incl, 31);
-            }
-            if (lane == 0) F[n_units] = ftot;
-            __syncwarp();
-            uint32_t jc = 0;     // first list not wholly issued
-            for (uint32_t p0 = 0; p0 < ftot; p0 += kBmPageIds, ++pg) {
-                const uint32_t p1 = min(p0 + kBmPageIds, ftot);
-                const uint32_t ps = pg % P;
-                if (lane == 0 && !mbar_wait(&empty[ps], ((pg / P) & 1u) ^ 1u)) abort = true;
-                abort = __shfl_sync(0xffffffffu, abort ? 1u : 0u, 0) != 0;
-                if (abort) break;
-                uint32_t *page = ring + ps * kBmPageIds;
-                uint32_t *pm = mask + ps * (kBmPageIds / 32);
-                const uint32_t cnt = p1 - p0;
-                for (uint32_t x = lane; x < kBmPageIds / 32; x += 32) {
-                    const uint32_t b0 = x * 32;
-                    pm[x] = b0 >= cnt ? 0u : (cnt - b0 >= 32 ? ~0u : (1u << (cnt - b0)) - 1u);
-                }
-                __syncwarp();
-                for (uint32_t j0 = jc; j0 < n_units && F[j0] < p1; j0 += 32) {
-                    const uint32_t j = j0 + lane;
-                    if (j < n_units) {
-                        const uint32_t fj = F[j], fe = F[j + 1];
-                        const uint32_t lo = max(fj, p0), hi = min(fe, p1);
-                        if (lo < hi) {
-                            const int64_t s = sstart[j], e = s + slen[j];
-                            const int64_t a = s & ~(int64_t)3;
-                            const uint32_t bytes = (hi - lo) * 4;
-                            if (GG_OK(a + (lo - fj) + (hi - lo) - 1, ix.n_ids + 4, 17)) {
-                                mbar_expect_tx(&full[ps], bytes);
-                                bulk_load(page + (lo - p0), ix.ids + a + (lo - fj), bytes, &full[ps]);
-                            }
-                            // the alignment padding before and after the list is not an id
-                            const uint32_t v0 = fj + (uint32_t)(s - a), v1 = v0 + (uint32_t)(e - s);
-                            for (uint32_t x = max(lo, fj); x < min(hi, v0); ++x)
-                                atomicAnd(&pm[(x - p0) >> 5], ~(1u << ((x - p0) & 31)));
-                            for (uint32_t x = max(lo, v1); x < min(hi, fe); ++x)
-                                atomicAnd(&pm[(x - p0) >> 5], ~(1u << ((x - p0) & 31)));
-                        }
-                    }
-                }
-                while (jc < n_units && F[jc + 1] <= p1) ++jc;
-                if (lane == 0) {
-                    BmPageHdr h;
-                    h.q = cur.q;
-                    h.k = cur.k;
-                    h.fill = cnt;
-                    h.last = p1 >= ftot ? 1u : 0u;
-                    h.out_off = cur.out_off;
-                    h.pad[0] = h.pad[1] = 0;
-                    hdr[ps] = h;
-                }
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&full[ps]);
-            }
-            if (lane == 0) {
-                cur = nxt;
-                nxt = after;
-            }
-        }
-        if (abort && lane == 0) {
-            atomicOr(&W.ctr[kCtrError], kErrTimeout);
-            s_abort = 1;
-            // let the copies already issued land before the block can exit
-            for (uint32_t b = pg > P ? pg - P : 0; b < pg; ++b) mbar_wait(&full[b % P], (b / P) & 1u, 10000000ull);
-        }
-        return;
-    }
-
-    // -------------------------------------------------------------- consumers
-    const uint32_t ct = tid - 32;
     const uint32_t mcap = mslots / 2;
     const uint32_t words = L.bm_words;
-    uint32_t *hist = ss.hist;
-    for (uint32_t i = ct; i < words / 4; i += kBmConsumers) ((uint4 *)bm)[i] = make_uint4(0u, 0u, 0u, 0u);
-    for (uint32_t i = ct; i < mslots; i += kBmConsumers) mt[i] = 0u;
-    for (uint32_t i = ct; i < 256; i += kBmConsumers) hist[i] = 0u;
-    BmConsumers::sync();
 
-    // a repeated id: count it in the table and the histogram; 1 for a new entry
-    auto repeat = [&](uint32_t id) -> uint32_t {
-        uint32_t h = slot_of(id, mslots);
-        for (uint32_t probe = 0; probe < kBmProbe; ++probe) {
-            uint32_t cur = mt[h];
-            if (cur == 0u) {
-                const uint32_t old = atomicCAS(&mt[h], 0u, (id << 8) | 2u);
-                if (old == 0u) {
-                    atomicAdd(&hist[2], 1u);
-                    return 1u;
-                }
-                cur = old;
-            }
-            if ((cur >> 8) == id) {
-                const uint32_t c = atomicAdd(&mt[h], 1u) & 255u;     // c + 1 <= 255: small-count query
-                atomicSub(&hist[c], 1u);
-                atomicAdd(&hist[c + 1], 1u);
-                return 0u;
-            }
-            h = (h + 1 == mslots) ? 0u : h + 1;
+    auto load_q = [&](uint32_t q) {      // thread 0
+        BmQuery d{};
+        d.q = q;
+        if (GG_OK(q, W.q_cap, 16)) {
+            const QInfo qi = W.qinfo[q];
+            d.k = qi.k;
+            d.n_units = (uint32_t)qi.n_units;
+            d.unit0 = qi.unit0;
+            d.out_off = Q.out_off[q];
         }
-        s_ovf = 1;
-        return 0u;
+        return d;
+    };
+    auto work_q = [&](uint32_t i) -> uint32_t {    // query of this CTA's i-th item, or ~0
+        const uint32_t w = blockIdx.x + i * G;
+        return (w < n_work && GG_OK(w, W.work_stride, 16)) ? work[w].x : 0xFFFFFFFFu;
     };
 
-    uint32_t pg = 0;
-    constexpr int R = (kBmPageIds + kBmConsumers - 1) / kBmConsumers;
-    for (uint32_t i = 0; blockIdx.x + i * G < n_work; ++i) {
-        uint32_t q = 0, k = 0;
-        int64_t out_off = 0;
-        bool first = true, aborted = false;
-        for (;;) {
-            const uint32_t ps = pg % P;
-            if (!mbar_wait(&full[ps], (pg / P) & 1u)) {
-                aborted = true;
-                break;
+    for (uint32_t i = tid; i < words / 4; i += kBmThreads) ((uint4 *)bm)[i] = make_uint4(0u, 0u, 0u, 0u);
+    for (uint32_t i = tid; i < mslots; i += kBmThreads) mt[i] = 0u;
+    for (uint32_t i = tid; i < 256; i += kBmThreads) hist[i] = 0u;
+    uint32_t q_next2 = 0xFFFFFFFFu;      // thread 0: query two items ahead
+    BmQuery qd_next{};                   // thread 0: descriptor one item ahead
+    if (tid == 0) {
+        s_multi = 0;
+        s_ovf = 0;
+        s_qd[0] = load_q(work_q(0));
+        const uint32_t q1 = work_q(1);
+        if (q1 != 0xFFFFFFFFu) qd_next = load_q(q1);
+        q_next2 = work_q(2);
+    }
+    __syncthreads();
+    // spans of this thread's list in the current query (prefetched one query ahead)
+    int64_t sp_start = 0, sp_len = 0;
+    if (tid < s_qd[0].n_units && GG_OK(s_qd[0].unit0 + tid, W.units_cap, 9)) {
+        sp_start = W.span_start[s_qd[0].unit0 + tid];
+        sp_len = W.span_len[s_qd[0].unit0 + tid];
+    }
+
+    for (uint32_t it = 0; blockIdx.x + it * G < n_work; ++it) {
+        const bool more = blockIdx.x + (it + 1) * G < n_work;
+        if (tid == 0 && more) s_qd[(it + 1) & 1] = qd_next;
+        // ---- stage: chunk entries of every list
+        const uint32_t nch = (uint32_t)((sp_len + 31) / 32);
+        uint32_t n_chunks = 0;
+        const uint32_t c0 = block_excl_scan(nch, ss.tmp, &n_chunks);     // ends with a barrier
+        const BmQuery d = s_qd[it & 1];
+        for (uint32_t c = 0; c < nch && c0 + c < kBmChunks; ++c) {
+            cstart[c0 + c] = sp_start + 32 * (int64_t)c;
+            ccnt[c0 + c] = (uint8_t)min((int64_t)32, sp_len - 32 * (int64_t)c);
+        }
+        // spans of the next query, in flight during this one
+        sp_start = 0;
+        sp_len = 0;
+        if (more) {
+            const BmQuery dn = s_qd[(it + 1) & 1];
+            if (tid < dn.n_units && GG_OK(dn.unit0 + tid, W.units_cap, 9)) {
+                sp_start = W.span_start[dn.unit0 + tid];
+                sp_len = W.span_len[dn.unit0 + tid];
             }
-            const BmPageHdr h = hdr[ps];
-            if (first) {
-                q = h.q;
-                k = h.k;
-                out_off = h.out_off;
-                first = false;
+        }
+        uint32_t q_next3 = 0xFFFFFFFFu;
+        if (tid == 0) q_next3 = work_q(it + 3);
+        __syncthreads();
+
+        // ---- stream
+        auto repeat = [&](uint32_t id) -> uint32_t {     // 1 for a new table entry
+            uint32_t h = slot_of(id, mslots);
+            for (uint32_t probe = 0; probe < kBmProbe; ++probe) {
+                uint32_t cur = mt[h];
+                if (cur == 0u) {
+                    const uint32_t old = atomicCAS(&mt[h], 0u, (id << 8) | 2u);
+                    if (old == 0u) {
+                        atomicAdd(&hist[2], 1u);
+                        return 1u;
+                    }
+                    cur = old;
+                }
+                if ((cur >> 8) == id) {
+                    const uint32_t c = atomicAdd(&mt[h], 1u) & 255u;     // c + 1 <= 255: small-count query
+                    atomicSub(&hist[c], 1u);
+                    atomicAdd(&hist[c + 1], 1u);
+                    return 0u;
+                }
+                h = (h + 1 == mslots) ? 0u : h + 1;
             }
-            const uint32_t *page = ring + ps * kBmPageIds;
-            const uint32_t *pm = mask + ps * (kBmPageIds / 32);
-            uint32_t v[R], old[R];
-            uint32_t ok = 0;
+            s_ovf = 1;
+            return 0u;
+        };
+        const uint32_t nc = min(n_chunks, kBmChunks);
+        for (uint32_t j0 = warp; j0 < nc; j0 += 32 * kBmRound) {
+            uint32_t v[kBmRound], ok = 0;
 #pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const uint32_t p = ct + r * kBmConsumers;
-                const bool in = p < h.fill;
-                const uint32_t mw = in ? pm[p >> 5] : 0u;
-                v[r] = in ? page[p] : 0u;
-                ok |= ((mw >> (p & 31)) & 1u) << r;
+            for (int r = 0; r < kBmRound; ++r) {
+                const uint32_t c = j0 + r * 32;
+                const bool inb = c < nc;
+                const int64_t st = inb ? cstart[c] : 0;
+                const uint32_t n = inb ? ccnt[c] : 0u;
+                const bool g = lane < n;
+                v[r] = __ldg(ix.ids + (g ? st + lane : 0));
+                ok |= (g ? 1u : 0u) << r;
             }
+            uint32_t old[kBmRound];
 #pragma unroll
-            for (int r = 0; r < R; ++r) {      // independent atomics, all in flight
+            for (int r = 0; r < kBmRound; ++r) {      // independent atomics, all in flight
                 bool g = (ok >> r & 1u) != 0;
                 g = g && GG_OK(v[r] >> 5, words, 15);
                 const uint32_t m = g ? 1u << (v[r] & 31) : 0u;
@@ -430,7 +258,7 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
             }
             uint32_t rep = 0;
 #pragma unroll
-            for (int r = 0; r < R; ++r) rep |= (old[r] != 0u ? 1u : 0u) << r;
+            for (int r = 0; r < kBmRound; ++r) rep |= (old[r] != 0u ? 1u : 0u) << r;
             uint32_t added = 0;
             while (__any_sync(0xffffffffu, rep != 0u)) {
                 if (rep) {
@@ -438,52 +266,45 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
                     rep &= rep - 1;
                     uint32_t id = v[0];
 #pragma unroll
-                    for (int j = 1; j < R; ++j) id = (r == (uint32_t)j) ? v[j] : id;
+                    for (int j = 1; j < kBmRound; ++j) id = (r == (uint32_t)j) ? v[j] : id;
                     added += repeat(id);
                 }
             }
             added = __reduce_add_sync(0xffffffffu, added);
             if (lane == 0 && added && atomicAdd(&s_multi, added) + added > mcap) s_ovf = 1;
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[ps]);
-            ++pg;
-            if (h.last) break;
         }
-        if (aborted && lane == 0) {
-            atomicOr(&W.ctr[kCtrError], kErrTimeout);
-            s_abort = 1;
-        }
-        BmConsumers::sync();
-        if (*(volatile uint32_t *)&s_abort) break;
+        if (tid == 0 && q_next2 != 0xFFFFFFFFu) qd_next = load_q(q_next2);     // lands during selection
+        __syncthreads();
 
         // ---- exact top-k of this query
+        const uint32_t k = d.k, q = d.q;
+        const int64_t out_off = d.out_off;
         const uint32_t n_multi = s_multi;
-        bool failed = s_ovf != 0;
-        uint32_t nres = 0;
-        uint32_t n_hi = 0;             // keys at cand[0, n_hi) first, then ties
+        bool failed = s_ovf != 0 || n_chunks > kBmChunks;
+        uint32_t nres = 0, n_hi = 0;
         const uint64_t *ties = cand;
         if (!failed && n_multi >= k) {
-            if (ct < 32) find_digit(ss, k, true);     // k-th largest count
-            if (ct == 0) {
+            if (warp == 0) find_digit(ss, k, true);     // k-th largest count
+            if (tid == 0) {
                 s_n = 0;
                 s_t = 0;
             }
-            BmConsumers::sync();
+            __syncthreads();
             const uint32_t cstar = ss.sc[0], above = ss.sc[1], n_eq = ss.sc[2];
             const uint32_t hp2 = next_pow2(above), tp2 = next_pow2(n_eq);
             if (hp2 + tp2 <= kCandCap) {
                 uint64_t *tie_buf = cand + hp2;
-                for (uint32_t b = 0; b < mslots; b += kBmConsumers) {
-                    const uint32_t x = b + ct;
+                for (uint32_t b = 0; b < mslots; b += kBmThreads) {
+                    const uint32_t x = b + tid;
                     const uint32_t e = x < mslots ? mt[x] : 0u;
                     const uint32_t c = e & 255u;
                     warp_append(e != 0u && c > cstar, make_key(c, e >> 8), cand, &s_n);
                     warp_append(e != 0u && c == cstar, make_key(c, e >> 8), tie_buf, &s_t);
                 }
-                for (uint32_t x = above + ct; x < hp2; x += kBmConsumers) cand[x] = 0ull;
-                for (uint32_t x = n_eq + ct; x < tp2; x += kBmConsumers) tie_buf[x] = 0ull;
-                bitonic_sort_desc<BmConsumers>(cand, hp2);
-                bitonic_sort_desc<BmConsumers>(tie_buf, tp2);
+                for (uint32_t x = above + tid; x < hp2; x += kBmThreads) cand[x] = 0ull;
+                for (uint32_t x = n_eq + tid; x < tp2; x += kBmThreads) tie_buf[x] = 0ull;
+                bitonic_sort_desc(cand, hp2);
+                bitonic_sort_desc(tie_buf, tp2);
                 n_hi = above;
                 ties = tie_buf;
                 nres = k;
@@ -492,27 +313,27 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
             }
         } else if (!failed) {
             // the whole table, then the smallest ids seen once
-            if (ct == 0) s_n = 0;
-            BmConsumers::sync();
-            for (uint32_t b = 0; b < mslots; b += kBmConsumers) {
-                const uint32_t x = b + ct;
+            if (tid == 0) s_n = 0;
+            __syncthreads();
+            for (uint32_t b = 0; b < mslots; b += kBmThreads) {
+                const uint32_t x = b + tid;
                 const uint32_t e = x < mslots ? mt[x] : 0u;
                 if (e) atomicAnd(&bm[(e >> 8) >> 5], ~(1u << ((e >> 8) & 31)));
                 warp_append(e != 0u, make_key(e & 255u, e >> 8), cand, &s_n);
             }
             const uint32_t np2 = next_pow2(n_multi);
-            BmConsumers::sync();
-            for (uint32_t x = n_multi + ct; x < np2; x += kBmConsumers) cand[x] = 0ull;
-            bitonic_sort_desc<BmConsumers>(cand, np2);
+            __syncthreads();
+            for (uint32_t x = n_multi + tid; x < np2; x += kBmThreads) cand[x] = 0ull;
+            bitonic_sort_desc(cand, np2);
             const uint32_t r = k - n_multi;
-            const uint32_t singles = bitmap_take_smallest<BmConsumers>(bm, words, r, 1u, cand + n_multi, ss);
+            const uint32_t singles = bitmap_take_smallest<BlockGroup>(bm, words, r, 1u, cand + n_multi, ss);
             n_hi = n_multi + min(r, singles);
             nres = n_hi;
         }
         if (failed) {
-            if (ct == 0) convert_to_dense(ix, W, T, q);
+            if (tid == 0) convert_to_dense(ix, W, T, q);
         } else {
-            for (uint32_t j = ct; j < k; j += kBmConsumers) {
+            for (uint32_t j = tid; j < k; j += kBmThreads) {
                 if (!GG_OK(out_off + j, W.out_cap, 4)) continue;
                 uint32_t id = 0, cnt = 0;
                 if (j < nres) {
@@ -526,15 +347,16 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
             }
         }
         // ---- clear the state for the next query
-        BmConsumers::sync();
-        for (uint32_t x = ct; x < words / 4; x += kBmConsumers) ((uint4 *)bm)[x] = make_uint4(0u, 0u, 0u, 0u);
-        for (uint32_t x = ct; x < mslots; x += kBmConsumers) mt[x] = 0u;
-        for (uint32_t x = ct; x < 256; x += kBmConsumers) hist[x] = 0u;
-        if (ct == 0) {
+        __syncthreads();
+        for (uint32_t x = tid; x < words / 4; x += kBmThreads) ((uint4 *)bm)[x] = make_uint4(0u, 0u, 0u, 0u);
+        for (uint32_t x = tid; x < mslots; x += kBmThreads) mt[x] = 0u;
+        for (uint32_t x = tid; x < 256; x += kBmThreads) hist[x] = 0u;
+        if (tid == 0) {
             s_multi = 0;
             s_ovf = 0;
+            q_next2 = q_next3;
         }
-        BmConsumers::sync();
+        __syncthreads();
     }
 }
 

@@ -23,8 +23,10 @@ constexpr int kCandCap = 2048;       // candidate buffer of the top-k selection
 
 enum : uint8_t { kClsNone = 0, kClsSparse = 1, kClsDense = 2 };
 enum : uint8_t { kFlagWeighted = 1, kFlagSmallCount = 2, kFlagRetry = 4, kFlagPacked = 8 };
-// posting lists a query may cover on the bitmap path (its span buffers)
-constexpr uint32_t kBmSpanCap = 256;
+// posting lists a query may cover on the bitmap path (one per thread)
+constexpr uint32_t kBmSpanCap = 1024;
+// posting ids of a query on the bitmap path (its 32-id chunk entries)
+constexpr uint32_t kBmMaxIds = 96 * 1024;
 
 enum : uint32_t { kErrWeight = 1, kErrOverflow = 2, kErrCapacity = 4, kErrUnits = 8, kErrTimeout = 16 };
 
@@ -93,7 +95,7 @@ struct Tuning {
     int32_t sparse_load_pct;       // posting ids per part <= this % of the hash slots
     int32_t bitmap_bits;           // largest id space of the bitmap kernel (0: off)
     int32_t bitmap_multi_slots;    // slots of its table of ids seen twice or more
-    int32_t bitmap_pages;          // its ring pages (set per launch from the id space)
+    int32_t bitmap_ready;          // 1 when its shared memory fits the id space (set per launch)
 };
 
 // Work lists, one per kernel variant.

@@ -202,8 +202,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_units(DevIndex ix, DevQue
             const int64_t cap = slots * T.sparse_load_pct / 100;     // table load factor bound
             const int64_t ps = (total + cap - 1) / cap;
             if (total <= T.sparse_max_total && total * 4 <= ix.n_objects * 3 && packed && !ix.codec &&
-                T.bitmap_bits > 0 && T.bitmap_pages >= 2 && ix.n_objects <= T.bitmap_bits &&
-                qi.n_units <= (int32_t)kBmSpanCap) {
+                T.bitmap_bits > 0 && T.bitmap_ready && ix.n_objects <= T.bitmap_bits &&
+                qi.n_units <= (int32_t)kBmSpanCap && total <= (int64_t)kBmMaxIds) {
                 // presence bitmap over the whole id space + a table of repeated ids
                 qi.cls = kClsSparse;
                 qi.parts = 1;
@@ -929,7 +929,7 @@ Tuning default_tuning() {
     t.sparse_load_pct = 50;
     t.bitmap_bits = 1179648;         // id spaces up to 144 KiB of presence bits
     t.bitmap_multi_slots = 4096;     // 16 KiB table of repeated ids
-    t.bitmap_pages = 0;              // set per launch
+    t.bitmap_ready = 0;              // set per launch
     return t;
 }
 
@@ -966,9 +966,9 @@ cudaError_t prepare_kernels_max() {
     return cudaSuccess;
 }
 
-// Ring pages of the bitmap kernel for an id space of n objects (0: the
-// bitmap, the table and two pages do not fit in shared memory).
-int bitmap_pages(const Tuning &t, int64_t n_objects) {
+// Whether the bitmap kernel's shared memory (bitmap, table, chunk entries)
+// fits for an id space of n objects under this tuning.
+bool bitmap_fits(const Tuning &t, int64_t n_objects) {
     static size_t limit = 0;
     if (!limit) {
         int dev = 0, optin = 0;
@@ -980,18 +980,16 @@ int bitmap_pages(const Tuning &t, int64_t n_objects) {
         if (cudaFuncGetAttributes(&a, (const void *)k_bitmap) == cudaSuccess) st = a.sharedSizeBytes;
         limit = (size_t)optin - st;
     }
-    if (t.bitmap_bits <= 0 || n_objects > t.bitmap_bits || t.bitmap_multi_slots <= 0) return 0;
-    for (int p = (int)kBmMaxPages; p >= 2; --p)
-        if (bm_layout(n_objects, (uint32_t)t.bitmap_multi_slots, (uint32_t)p).bytes <= limit) return p;
-    return 0;
+    if (t.bitmap_bits <= 0 || n_objects > t.bitmap_bits || t.bitmap_multi_slots <= 0) return false;
+    return bm_layout(n_objects, (uint32_t)t.bitmap_multi_slots).bytes <= limit;
 }
 
 int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &tun,
                  int num_sms, cudaStream_t s, cudaEvent_t *ev) {
     if (Q.n_queries <= 0) return 0;
     Tuning t = tun;
-    t.bitmap_pages = bitmap_pages(t, ix.n_objects);
-    if (t.bitmap_pages < 2) t.bitmap_bits = 0;
+    t.bitmap_ready = bitmap_fits(t, ix.n_objects) ? 1 : 0;
+    if (!t.bitmap_ready) t.bitmap_bits = 0;
     int launches = 0;
     if (ev) cudaEventRecord(ev[0], s);
     cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), s);
@@ -1009,7 +1007,7 @@ int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const T
     const size_t sp = sparse_smem_bytes(t, true), sw = sparse_smem_bytes(t, false);
     const size_t dp = dense_smem_bytes(t, true), dw = dense_smem_bytes(t, false);
     if (t.bitmap_bits > 0) {
-        const size_t bp = bm_layout(ix.n_objects, (uint32_t)t.bitmap_multi_slots, (uint32_t)t.bitmap_pages).bytes;
+        const size_t bp = bm_layout(ix.n_objects, (uint32_t)t.bitmap_multi_slots).bytes;
         k_bitmap<<<num_sms, kBmThreads, bp, s>>>(ix, Q, W, t);
     }
     if (ev) cudaEventRecord(ev[2], s);

@@ -22,8 +22,8 @@ cudaError_t prepare_kernels_max();
 // i+1 is recorded after stage i: plan, bitmap, sparse-packed, sparse-wide,
 // dense-small, dense-wide (event 0 before the plan).
 constexpr int kStages = 6;
-// Ring pages of the bitmap kernel for an id space of n objects (0: path off).
-int bitmap_pages(const Tuning &t, int64_t n_objects);
+// Whether the bitmap kernel's shared memory fits an id space of n objects.
+bool bitmap_fits(const Tuning &t, int64_t n_objects);
 int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t,
                  int num_sms, cudaStream_t s, cudaEvent_t *ev = nullptr);
 
