@@ -37,7 +37,7 @@ constexpr int kBmRound = 16;              // chunk loads in flight per lane
 
 // Byte offsets of the shared-memory regions (host and device agree).
 struct BmLayout {
-    uint32_t bm, mt, cstart, ccnt, ss, bytes, bm_words;
+    uint32_t bm, mt, mlist, cstart, ccnt, ss, bytes, bm_words;
 };
 __host__ __device__ inline uint32_t bm_align(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
 __host__ __device__ inline BmLayout bm_layout(int64_t n_objects, uint32_t mslots) {
@@ -46,6 +46,7 @@ __host__ __device__ inline BmLayout bm_layout(int64_t n_objects, uint32_t mslots
     L.bm_words = (uint32_t)((n_objects + 127) / 128) * 4;
     L.bm = o;     o += bm_align(L.bm_words * 4, 128);
     L.mt = o;     o += bm_align(mslots * 4, 128);
+    L.mlist = o;  o += bm_align(mslots / 2 * 4, 128);     // slots of the table's entries
     L.cstart = o; o += kBmChunks * 8;      // also the candidate keys after streaming
     L.ccnt = o;   o += kBmChunks;
     L.ss = o;     o += bm_align((uint32_t)sizeof(SelectScratch), 16);
@@ -133,10 +134,13 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
     uint32_t *mt = (uint32_t *)(smem + L.mt);
     int64_t *cstart = (int64_t *)(smem + L.cstart);
     uint8_t *ccnt = smem + L.ccnt;
-    uint64_t *cand = (uint64_t *)(smem + L.cstart);
+    uint32_t *mlist = (uint32_t *)(smem + L.mlist);
+    uint64_t *cand = (uint64_t *)(smem + L.cstart);                  // [0, kCandCap)
+    uint32_t *tie_ids = (uint32_t *)(cand + kCandCap);               // [0, kCandCap)
+    uint64_t *tie_keys = cand + kCandCap + kCandCap / 2;             // [0, kCandCap / 2)
     SelectScratch &ss = *(SelectScratch *)(smem + L.ss);
     uint32_t *hist = ss.hist;
-    __shared__ uint32_t s_multi, s_ovf, s_n, s_t;
+    __shared__ uint32_t s_multi, s_ovf, s_n, s_big;
     __shared__ uint32_t s_spare[32];
     __shared__ BmQuery s_qd[2];
 
@@ -220,6 +224,9 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
                     const uint32_t old = atomicCAS(&mt[h], 0u, (id << 8) | 2u);
                     if (old == 0u) {
                         atomicAdd(&hist[2], 1u);
+                        const uint32_t at = atomicAdd(&s_multi, 1u);
+                        if (at < mcap) mlist[at] = h;
+                        else s_ovf = 1;
                         return 1u;
                     }
                     cur = old;
@@ -259,7 +266,6 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
             uint32_t rep = 0;
 #pragma unroll
             for (int r = 0; r < kBmRound; ++r) rep |= (old[r] != 0u ? 1u : 0u) << r;
-            uint32_t added = 0;
             while (__any_sync(0xffffffffu, rep != 0u)) {
                 if (rep) {
                     const uint32_t r = __ffs(rep) - 1;
@@ -267,11 +273,9 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
                     uint32_t id = v[0];
 #pragma unroll
                     for (int j = 1; j < kBmRound; ++j) id = (r == (uint32_t)j) ? v[j] : id;
-                    added += repeat(id);
+                    repeat(id);
                 }
             }
-            added = __reduce_add_sync(0xffffffffu, added);
-            if (lane == 0 && added && atomicAdd(&s_multi, added) + added > mcap) s_ovf = 1;
         }
         if (tid == 0 && q_next2 != 0xFFFFFFFFu) qd_next = load_q(q_next2);     // lands during selection
         __syncthreads();
@@ -279,45 +283,88 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
         // ---- exact top-k of this query
         const uint32_t k = d.k, q = d.q;
         const int64_t out_off = d.out_off;
-        const uint32_t n_multi = s_multi;
+        const uint32_t n_multi = min(s_multi, mcap);
         bool failed = s_ovf != 0 || n_chunks > kBmChunks;
-        uint32_t nres = 0, n_hi = 0;
-        const uint64_t *ties = cand;
+        uint32_t nres = 0, n_hi = 0, cstar = 0;     // keys cand[0, n_hi), then tie ids at c*
         if (!failed && n_multi >= k) {
             if (warp == 0) find_digit(ss, k, true);     // k-th largest count
             if (tid == 0) {
                 s_n = 0;
-                s_t = 0;
+                s_big = 0;
             }
             __syncthreads();
-            const uint32_t cstar = ss.sc[0], above = ss.sc[1], n_eq = ss.sc[2];
-            const uint32_t hp2 = next_pow2(above), tp2 = next_pow2(n_eq);
-            if (hp2 + tp2 <= kCandCap) {
-                uint64_t *tie_buf = cand + hp2;
-                for (uint32_t b = 0; b < mslots; b += kBmThreads) {
-                    const uint32_t x = b + tid;
-                    const uint32_t e = x < mslots ? mt[x] : 0u;
-                    const uint32_t c = e & 255u;
-                    warp_append(e != 0u && c > cstar, make_key(c, e >> 8), cand, &s_n);
-                    warp_append(e != 0u && c == cstar, make_key(c, e >> 8), tie_buf, &s_t);
-                }
-                for (uint32_t x = above + tid; x < hp2; x += kBmThreads) cand[x] = 0ull;
-                for (uint32_t x = n_eq + tid; x < tp2; x += kBmThreads) tie_buf[x] = 0ull;
-                bitonic_sort_desc(cand, hp2);
-                bitonic_sort_desc(tie_buf, tp2);
-                n_hi = above;
-                ties = tie_buf;
-                nres = k;
-            } else {
-                failed = true;
+            cstar = ss.sc[0];
+            const uint32_t above = ss.sc[1], n_eq = ss.sc[2];
+            // tie ids go to id-range buckets (counting sort): bucket b holds ids
+            // [b << sh, (b+1) << sh); the counters borrow the first bitmap words
+            const uint32_t nb = min(1024u, words);
+            uint32_t sh = 0;
+            while (((uint32_t)(ix.n_objects - 1) >> sh) >= nb) ++sh;
+            uint32_t *bcnt = bm;
+            for (uint32_t x = tid; x < nb; x += kBmThreads) bcnt[x] = 0u;
+            __syncthreads();
+            // entries above c* to cand (warp-aggregated); count the ties per bucket
+            for (uint32_t b = 0; b < n_multi; b += kBmThreads) {
+                const uint32_t x = b + tid;
+                const uint32_t e = x < n_multi ? mt[mlist[x]] : 0u;
+                const uint32_t c = e & 255u;
+                warp_append(e != 0u && c > cstar, make_key(c, e >> 8), cand, &s_n);
+                if (e != 0u && c == cstar) atomicAdd(&bcnt[(e >> 8) >> sh], 1u);
             }
+            __syncthreads();
+            const uint32_t bc = tid < nb ? bcnt[tid] : 0u;
+            if (bc > 32) s_big = 1;      // a crowded id range: sort all ties instead
+            uint32_t tot = 0;
+            const uint32_t boff = block_excl_scan(bc, ss.tmp, &tot);     // ends with a barrier
+            if (tid < nb) bcnt[tid] = boff;                              // cursor
+            __syncthreads();
+            for (uint32_t b = 0; b < n_multi; b += kBmThreads) {
+                const uint32_t x = b + tid;
+                const uint32_t e = x < n_multi ? mt[mlist[x]] : 0u;
+                if (e != 0u && (e & 255u) == cstar) {
+                    const uint32_t at = atomicAdd(&bcnt[(e >> 8) >> sh], 1u);
+                    if (GG_OK(at, kCandCap, 19)) tie_ids[at] = e >> 8;
+                }
+            }
+            if (warp == 0 && above <= 64) warp_sort_desc64(cand, above);
+            __syncthreads();
+            if (above > 64) {
+                const uint32_t hp2 = next_pow2(above);
+                for (uint32_t x = above + tid; x < hp2; x += kBmThreads) cand[x] = 0ull;
+                bitonic_sort_desc(cand, hp2);
+            }
+            const bool big = s_big != 0;
+            if (big && next_pow2(n_eq) <= kCandCap / 2) {
+                const uint32_t tp2 = next_pow2(n_eq);
+                for (uint32_t x = tid; x < tp2; x += kBmThreads)
+                    tie_keys[x] = x < n_eq ? make_key(cstar, tie_ids[x]) : 0ull;
+                bitonic_sort_desc(tie_keys, tp2);     // one count: ascending ids
+                for (uint32_t x = tid; x < n_eq; x += kBmThreads) tie_ids[x] = key_id(tie_keys[x]);
+            } else if (big) {
+                failed = true;
+            } else if (tid < nb && bc > 1) {      // each bucket in id order (a few ids each)
+                uint32_t *bk = tie_ids + boff;
+                for (uint32_t i = 1; i < bc; ++i) {
+                    const uint32_t x = bk[i];
+                    uint32_t j = i;
+                    while (j > 0 && bk[j - 1] > x) {
+                        bk[j] = bk[j - 1];
+                        --j;
+                    }
+                    bk[j] = x;
+                }
+            }
+            __syncthreads();
+            n_hi = above;
+            nres = k;
+            if (n_eq != tot || n_eq > kCandCap) failed = true;
         } else if (!failed) {
             // the whole table, then the smallest ids seen once
             if (tid == 0) s_n = 0;
             __syncthreads();
-            for (uint32_t b = 0; b < mslots; b += kBmThreads) {
+            for (uint32_t b = 0; b < n_multi; b += kBmThreads) {
                 const uint32_t x = b + tid;
-                const uint32_t e = x < mslots ? mt[x] : 0u;
+                const uint32_t e = x < n_multi ? mt[mlist[x]] : 0u;
                 if (e) atomicAnd(&bm[(e >> 8) >> 5], ~(1u << ((e >> 8) & 31)));
                 warp_append(e != 0u, make_key(e & 255u, e >> 8), cand, &s_n);
             }
@@ -337,9 +384,14 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
                 if (!GG_OK(out_off + j, W.out_cap, 4)) continue;
                 uint32_t id = 0, cnt = 0;
                 if (j < nres) {
-                    const uint64_t key = j < n_hi ? cand[j] : ties[j - n_hi];
-                    id = key_id(key);
-                    cnt = key_prim(key);
+                    if (j < n_hi) {
+                        const uint64_t key = cand[j];
+                        id = key_id(key);
+                        cnt = key_prim(key);
+                    } else {
+                        id = tie_ids[j - n_hi];
+                        cnt = cstar;
+                    }
                 }
                 W.out_ids[out_off + j] = id;
                 W.out_counts[out_off + j] = cnt;
@@ -349,8 +401,13 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
         // ---- clear the state for the next query
         __syncthreads();
         for (uint32_t x = tid; x < words / 4; x += kBmThreads) ((uint4 *)bm)[x] = make_uint4(0u, 0u, 0u, 0u);
-        for (uint32_t x = tid; x < mslots; x += kBmThreads) mt[x] = 0u;
+        if (s_ovf) {
+            for (uint32_t x = tid; x < mslots; x += kBmThreads) mt[x] = 0u;
+        } else {
+            for (uint32_t x = tid; x < min(s_multi, mcap); x += kBmThreads) mt[mlist[x]] = 0u;
+        }
         for (uint32_t x = tid; x < 256; x += kBmThreads) hist[x] = 0u;
+        __syncthreads();     // s_multi read above before it is reset
         if (tid == 0) {
             s_multi = 0;
             s_ovf = 0;

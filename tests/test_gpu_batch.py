@@ -129,6 +129,26 @@ def test_bitmap_overflow_retries_dense(genie, oracle):
     assert np.array_equal(ids, oid) and np.array_equal(cnt, ocnt)
 
 
+def test_bitmap_ties_in_one_id_range(genie, oracle):
+    """Many ids tied at the k-th count inside one small id range (identical
+    objects with adjacent ids) are still returned in ascending id order."""
+    rng = np.random.default_rng(11)
+    values = rng.integers(0, 1000, size=(100_000, 16), dtype=np.int32)
+    values[:40] = values[0]
+    q = 6
+    dims = np.tile(np.arange(16, dtype=np.int32), q)
+    vals = rng.integers(0, 1000, size=(q, 16)).astype(np.int32)
+    vals[:, :5] = values[0, :5]
+    vals = vals.ravel()
+    qb = genie.QueryBatch(np.arange(q + 1) * 16, dims, vals, vals, 10)
+    t = genie.Table.from_values(values)
+    bt = genie.Batch(t, q, q * 16, 10)
+    ids, cnt = bt.run(qb)
+    oid, ocnt, _, _ = oracle.Index(values).search(qb.as_oracle_batch())
+    assert np.array_equal(ids, oid) and np.array_equal(cnt, ocnt)
+    assert list(ids[:10]) == list(range(10))
+
+
 def test_batch_capacity_errors(genie):
     t = genie.Table.from_values(np.zeros((10, 2), np.int32))
     bt = genie.Batch(t, 2, 4, 5)
