@@ -22,7 +22,7 @@ from ._lib import GenieQueries, GenieIndexInfo
 __all__ = [
     "Config", "MakePolicy", "ExecutionPolicy", "Search", "BuildTable", "BuildQuery", "Match",
     "LoadTableDataFromCsv", "LoadQueryDataFromCsv", "LoadTableFromBinary", "SaveTableToBinary",
-    "Table", "Query", "QueryBatch", "Batch", "search", "lib",
+    "Table", "Query", "QueryBatch", "Batch", "Server", "poisson_arrivals", "search", "lib",
     "NotImplementedException", "InvalidConfigurationException", "gpu_bad_alloc", "gpu_runtime_error",
     "cpu_bad_alloc", "cpu_runtime_error",
 ]
@@ -508,3 +508,4 @@ def Search(policy, table_filename, query_filename):
 
 
 from .batch import Batch  # noqa: E402
+from .serve import Server, poisson_arrivals  # noqa: E402

@@ -35,6 +35,17 @@ class GenieTuning(ctypes.Structure):
                 ("sparse_load_pct", I32), ("bitmap_bits", I32)]
 
 
+class GenieServerConfig(ctypes.Structure):
+    _fields_ = [("slots_per_index", I32), ("max_queries", I32), ("max_items", I64), ("max_k", U32),
+                ("window_us", I32), ("memory_budget", I64)]
+
+
+class GenieServerReport(ctypes.Structure):
+    _fields_ = [("submitted", I64), ("completed", I64), ("rejected", I64), ("batches", I64),
+                ("mean_batch", ctypes.c_double), ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double),
+                ("max_us", ctypes.c_double), ("throughput_qps", ctypes.c_double)]
+
+
 # name -> (restype, argtypes); mirrors include/genie_gb300.h
 PROTOTYPES = {
     "genie_last_error": (ctypes.c_char_p, []),
@@ -65,6 +76,16 @@ PROTOTYPES = {
     "genie_batch_set_tuning": (ctypes.c_int, [P, P]),
     "genie_batch_last_stats": (ctypes.c_int, [P, P, P]),
     "genie_batch_stage_ms": (ctypes.c_int, [P, P]),
+    "genie_server_create": (ctypes.c_int, [P, P]),
+    "genie_server_add_index": (ctypes.c_int, [P, P, P]),
+    "genie_server_start": (ctypes.c_int, [P]),
+    "genie_server_submit": (ctypes.c_int, [P, I32, P, P, P]),
+    "genie_server_wait": (ctypes.c_int, [P, ctypes.c_uint64, P, P, P, P]),
+    "genie_server_drain": (ctypes.c_int, [P]),
+    "genie_server_stats": (ctypes.c_int, [P, P]),
+    "genie_server_reset_stats": (ctypes.c_int, [P]),
+    "genie_server_now_ns": (I64, []),
+    "genie_server_destroy": (ctypes.c_int, [P]),
     "genie_codec_encode": (I64, [I32, P, I64, P, I64]),
     "genie_codec_encode_bound": (I64, [I64]),
     "genie_codec_decode_device": (ctypes.c_int, [I32, P, P, I64, P, P, P, P]),

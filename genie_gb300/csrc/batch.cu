@@ -408,3 +408,30 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- serving steps
+
+int gg::batch_submit_async(genie_batch *b, const genie_queries *q, bool scores) {
+    cudaSetDevice(b->ix->device);
+    int rc = stage_async(b, q, b->stream);
+    if (rc) return rc;
+    cudaEventRecord(b->ev0, b->stream);
+    rc = enqueue(b, b->stream);
+    b->launched = rc == GENIE_OK;
+    if (rc) return rc;
+    rc = fetch_async(b, b->stream, scores);
+    if (rc) return rc;
+    cudaError_t e = cudaEventRecord(b->ev1, b->stream);
+    return e ? cuda_fail(e, "batch event") : GENIE_OK;
+}
+
+int gg::batch_ready(genie_batch *b) {
+    cudaError_t e = cudaEventQuery(b->ev1);
+    if (e == cudaSuccess) return 1;
+    if (e == cudaErrorNotReady) return 0;
+    return -cuda_fail(e, "batch");
+}
+
+int gg::batch_collect(genie_batch *b, uint32_t *ids, uint32_t *counts, float *scores) {
+    return finish_fetch(b, ids, counts, scores);
+}

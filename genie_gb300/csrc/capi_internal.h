@@ -48,6 +48,12 @@ struct Workspace {
 };
 
 int validate_queries(const genie_queries *q, std::vector<int64_t> &out_off, int64_t &n_items);
+
+// Asynchronous steps of one batch for the serving loop (batch.cu): stage,
+// launch and download on the batch's own stream; poll; copy the results out.
+int batch_submit_async(genie_batch *b, const genie_queries *q, bool scores);
+int batch_ready(genie_batch *b);      // 1 done, 0 still running, < 0 a CUDA error
+int batch_collect(genie_batch *b, uint32_t *ids, uint32_t *counts, float *scores);
 int check_device_error(uint32_t err);
 int64_t count_units(const HostIndex &h, const genie_queries *q);
 

@@ -231,6 +231,60 @@ int genie_batch_last_stats(const genie_batch *b, int32_t *kernels, float *device
  * ms[4] dense 1-byte-counter kernel, ms[5] dense 4-byte-counter kernel. */
 int genie_batch_stage_ms(const genie_batch *b, float *ms);
 
+/* ---------------------------------------------------------------- serving */
+
+/* A request loop over several resident indexes with continuous batching.
+ * Requests (one query each) are admitted when a batch slot of their index is
+ * free and their memory estimate fits the budget; the requests that have
+ * arrived by then form the slot's batch, which runs while other slots' batches
+ * are still on the device, so requests that arrive during a run join the next
+ * free slot instead of waiting for a whole queue to drain.  A scheduler thread
+ * owned by the server does the batching, launches and completions; callers
+ * only submit and wait.
+ * Reference counterpart: the memory-budget admission loop of knn_MT
+ * (matching/knn.cu:206-278) and the request loop of odgenie
+ * (dist_genie/online.cu:37-180, scheduler.cc:20-64), which runs one request
+ * as one synchronous batch. */
+typedef struct {
+    int32_t slots_per_index;  /* batches of one index that may be on the device at once (>= 1) */
+    int32_t max_queries;      /* requests per batch */
+    int64_t max_items;        /* items per batch */
+    uint32_t max_k;
+    int32_t window_us;        /* while a slot of the index is busy, wait up to this long for more requests */
+    int64_t memory_budget;    /* bytes of in-flight request state; 0: bounded by the slots alone */
+} genie_server_config;
+
+typedef struct {
+    int64_t submitted, completed, rejected, batches;
+    double mean_batch;        /* requests per batch */
+    double p50_us, p99_us, max_us;   /* arrival -> result ready, completed requests since the last reset */
+    double throughput_qps;    /* completed / (last completion - first arrival) */
+} genie_server_report;
+
+int genie_server_create(const genie_server_config *cfg, genie_server **out);
+/* Make an index servable (before genie_server_start); the index must outlive
+ * the server. */
+int genie_server_add_index(genie_server *s, genie_index *ix, int32_t *index_id);
+int genie_server_start(genie_server *s);
+/* Submit q->n_queries requests (one per query) to index index_id.  Request i
+ * counts as arriving at arrival_ns[i] on the genie_server_now_ns clock
+ * (arrival_ns NULL: all now); future times schedule the requests.  Tickets
+ * are *first_ticket, +1, ...  A request that can never be admitted (items, k
+ * or memory beyond the configuration) fails the whole call with
+ * GENIE_ERR_ADMISSION. */
+int genie_server_submit(genie_server *s, int32_t index_id, const genie_queries *q, const int64_t *arrival_ns,
+                        uint64_t *first_ticket);
+/* Block until the request is answered; copy its k ids, counts and (optional)
+ * scores; release the ticket.  latency_ns (optional) = completion - arrival. */
+int genie_server_wait(genie_server *s, uint64_t ticket, uint32_t *out_ids, uint32_t *out_counts,
+                      float *out_scores, int64_t *latency_ns);
+/* Block until every submitted request is answered. */
+int genie_server_drain(genie_server *s);
+int genie_server_stats(genie_server *s, genie_server_report *out);
+int genie_server_reset_stats(genie_server *s);
+int64_t genie_server_now_ns(void);
+int genie_server_destroy(genie_server *s);
+
 /* ---------------------------------------------------------------- codecs */
 
 /* Host encoder of the reference byte formats (DeviceCodecFactory.cu:13-48).
