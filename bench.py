@@ -51,6 +51,10 @@ def parse():
     p.add_argument("--queries", type=int, default=1024)
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-autotune", action="store_true")
+    p.add_argument("--no-serve", action="store_true", help="skip the serving (config 4) leg")
+    p.add_argument("--serve-objects", type=int, default=1_000_000,
+                   help="objects of the config2/config3 indexes resident beside config1 while serving")
+    p.add_argument("--serve-seconds", type=float, default=0.2, help="arrival window per offered rate")
     p.add_argument("--tuning", default="",
                    help="fixed kernel shape, e.g. sparse_slots=53248,sparse_ctas_per_sm=1 (skips autotuning)")
     return p.parse_args()
@@ -163,6 +167,75 @@ def max_over_ranks(x, dist, device_is_cuda):
     t = torch.tensor([x], dtype=torch.float64, device="cuda" if device_is_cuda else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def serve_leg(g, workloads, t1, b1, args):
+    """Config 4 (serving): the config1 index plus config3 and config2 indexes
+    (the latter compressed with SERIAL_DELTA_COMP_BP32_VARINT in 128-id
+    segments) resident together; open-loop Poisson arrivals at 10k, 50k and
+    200k requests/s drawn 2:1:1 from the config3 : config1 : config2 query
+    generators; one query per request.  Latency = answer ready - arrival.
+    Beside it, the same request mix through the plain per-batch path
+    (genie_search, 256 queries per call)."""
+    import numpy as np
+    v3, b3 = workloads.config3(n=args.serve_objects, q=4096)
+    v2, b2 = workloads.config2(n=args.serve_objects, q=4096, k=32)
+    t3 = g.Table.from_values(v3)
+    t2 = g.Table.compressed(v2, 13, 128)
+    del v3, v2
+    srv = g.Server(max_queries=256, max_items=256 * 240, max_k=100, slots_per_index=2, window_us=100)
+    tables = [t1, t3, t2]
+    pools = [b1, b3, b2]
+    ids = [srv.add_index(t) for t in tables]
+    srv.start()
+    rates = {}
+    last_mix = None
+    for rate in (10_000, 50_000, 200_000):
+        n = max(64, int(rate * args.serve_seconds))
+        rng = np.random.default_rng(rate)
+        which = rng.choice(np.array([1, 1, 0, 2]), size=n)         # 2:1:1 config3 : config1 : config2
+        start = srv.now_ns() + 200_000_000 + n * 3_000             # after every submission below
+        arrivals = g.poisson_arrivals(rate, n, seed=rate + 1, start_ns=start)
+        srv.reset_stats()
+        subs, mix = [], []
+        for j in range(3):
+            sel = np.nonzero(which == j)[0]
+            if sel.size == 0:
+                continue
+            qs = rng.integers(0, pools[j]["k"].shape[0], sel.size)
+            sub = workloads.take_queries(pools[j], qs)
+            qb = g.QueryBatch(sub["item_off"], sub["dim"], sub["low"], sub["up"], sub["k"], sub["weight"],
+                              sub["weighted"])
+            first = srv.submit(ids[j], qb, arrivals[sel])
+            subs.append((first, qb.k_array))
+            mix.append((j, sub))
+        srv.drain()
+        st = srv.stats()
+        for first, ks in subs:
+            for i, k in enumerate(ks):
+                srv.wait(first + i, int(k))
+        rates[str(rate)] = {"offered_qps": rate, "requests": n, "sustained_qps": st["throughput_qps"],
+                            "p50_us": st["p50_us"], "p99_us": st["p99_us"], "max_us": st["max_us"],
+                            "mean_batch": st["mean_batch"]}
+        last_mix = mix
+    srv.close()
+    # the same last mix through the plain per-batch path
+    t0 = time.perf_counter()
+    n_plain = 0
+    for j, sub in last_mix:
+        Qj = sub["k"].shape[0]
+        for q0 in range(0, Qj, 256):
+            part = workloads.take_queries(sub, np.arange(q0, min(Qj, q0 + 256)))
+            qb = g.QueryBatch(part["item_off"], part["dim"], part["low"], part["up"], part["k"], part["weight"],
+                              part["weighted"])
+            g.search(tables[j], qb)
+            n_plain += qb.n_queries
+    plain_qps = n_plain / (time.perf_counter() - t0)
+    return {"indexes": "config1 %d x 240; config3 %d x 128; config2 %d x 32 compressed" % (
+                t1.i_size(), args.serve_objects, args.serve_objects),
+            "mix": "2:1:1 config3 : config1 : config2, one query per request, Poisson arrivals",
+            "rates": rates, "plain_per_batch_qps": plain_qps,
+            "served_over_plain_at_200k": rates["200000"]["sustained_qps"] / plain_qps}
 
 
 def run_reference(args, world, rank):
@@ -341,6 +414,10 @@ def main():
                          % (Q, reps, t_build),
                "matches_gpu": bool(np.array_equal(oid, ids_graph) and np.array_equal(ocnt, cnt_graph))}
 
+    serving = None
+    if rank == 0 and not args.no_serve:
+        serving = serve_leg(g, workloads, table, batch, args)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
@@ -355,6 +432,7 @@ def main():
                           "batched_over_plain": e2e / plain, "same_results": same},
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "serving": serving,
             "clocks": clock_info,
             "gpu_launches": kernels_per_step * args.steps,
         }

@@ -119,3 +119,20 @@ def algorithmic_bytes(key_offsets, key_base, dim_min, dim_max, batch, bytes_per_
     k1 = np.where(ok, k1, 0)
     spans = np.where(ok, key_offsets[k1] - key_offsets[k0], 0)
     return int(spans.sum()) * bytes_per_id
+
+
+def take_queries(batch, qs):
+    """The batch made of queries qs (indices, repeats allowed) of `batch`."""
+    qs = np.asarray(qs, np.int64)
+    off = batch["item_off"]
+    lens = off[qs + 1] - off[qs]
+    new_off = np.zeros(len(qs) + 1, np.int64)
+    np.cumsum(lens, out=new_off[1:])
+    src = np.repeat(off[qs] - new_off[:-1], lens) + np.arange(new_off[-1])
+    out = dict(item_off=new_off, dim=batch["dim"][src], low=batch["low"][src], up=batch["up"][src],
+               k=batch["k"][qs], weight=None, weighted=None)
+    if batch.get("weight") is not None:
+        out["weight"] = batch["weight"][src]
+        out["weighted"] = batch["weighted"][qs]
+    return out
+
