@@ -96,6 +96,7 @@ struct Tuning {
     int32_t bitmap_bits;           // largest id space of the bitmap kernel (0: off)
     int32_t bitmap_multi_slots;    // slots of its table of ids seen twice or more
     int32_t bitmap_ready;          // 1 when its shared memory fits the id space (set per launch)
+    int32_t num_sms;               // SMs of the device (set per launch)
 };
 
 // Work lists, one per kernel variant.

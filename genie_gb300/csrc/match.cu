@@ -41,6 +41,20 @@ void read_oob(unsigned long long out[4]) {
 
 constexpr int kPlanThreads = 128;
 
+// Id-range parts of a dense query: one per dense_part_work posting ids, more
+// when the batch has too few queries to give every SM a part, at most one per
+// tile and kMaxParts.
+__device__ __forceinline__ int64_t dense_parts(int64_t total, int64_t ntiles, int64_t nq, const Tuning &T) {
+    int64_t pd = (total + T.dense_part_work - 1) / T.dense_part_work;
+    if (T.num_sms > 0 && nq > 0) {
+        const int64_t fill = (T.num_sms + nq - 1) / nq;
+        pd = pd > fill ? pd : fill;
+    }
+    pd = pd > ntiles ? ntiles : pd;
+    pd = pd > kMaxParts ? kMaxParts : pd;
+    return pd < 1 ? 1 : pd;
+}
+
 __global__ void __launch_bounds__(kPlanThreads) k_plan_items(DevIndex ix, DevQueries Q, Work W, Tuning T) {
     __shared__ unsigned long long s_total, s_units;
     __shared__ unsigned int s_maxw, s_bad;
@@ -218,11 +232,7 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_units(DevIndex ix, DevQue
                 qi.cls = kClsDense;
                 const int64_t tile = small ? T.dense_tile_u8 : T.dense_tile_u32;
                 const int64_t ntiles = (ix.n_objects + tile - 1) / tile;
-                int64_t pd = (total + T.dense_part_work - 1) / T.dense_part_work;
-                pd = pd < 1 ? 1 : pd;
-                pd = pd > ntiles ? ntiles : pd;
-                pd = pd > kMaxParts ? kMaxParts : pd;
-                qi.parts = (uint16_t)pd;
+                qi.parts = (uint16_t)dense_parts(total, ntiles, nq, T);
                 list = small ? kListDenseSmall : kListDenseWide;
             }
         }
@@ -508,14 +518,12 @@ __device__ void convert_to_dense(const DevIndex &ix, const Work &W, const Tuning
     const bool small = (qi.flags & kFlagSmallCount) != 0;
     const int64_t tile = small ? T.dense_tile_u8 : T.dense_tile_u32;
     const int64_t ntiles = (ix.n_objects + tile - 1) / tile;
-    int64_t pd = (qi.total + T.dense_part_work - 1) / T.dense_part_work;
-    pd = pd < 1 ? 1 : pd;
-    pd = pd > ntiles ? ntiles : pd;
-    pd = pd > kMaxParts ? kMaxParts : pd;
+    const int64_t pd = dense_parts(qi.total, ntiles, 1, T);
     qi.parts = (uint16_t)pd;
     qi.cls = kClsDense;
     W.qinfo[q] = qi;
     W.done[q] = 0;
+    W.qstate[q] = 0;         // the dense parts' merge must not see the sparse overflow again
     const int list = small ? kListDenseSmall : kListDenseWide;
     uint2 *wl = W.work + (size_t)list * W.work_stride;
     uint32_t base = atomicAdd(&W.ctr[2 * list], (uint32_t)pd);
@@ -988,6 +996,7 @@ int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const T
                  int num_sms, cudaStream_t s, cudaEvent_t *ev) {
     if (Q.n_queries <= 0) return 0;
     Tuning t = tun;
+    t.num_sms = num_sms;
     t.bitmap_ready = bitmap_fits(t, ix.n_objects) ? 1 : 0;
     if (!t.bitmap_ready) t.bitmap_bits = 0;
     int launches = 0;
