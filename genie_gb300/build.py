@@ -87,5 +87,60 @@ def build(force=False, verbose=False):
     return LIB
 
 
+CPP = os.path.join(HERE, "cpp")
+CPP_LIB = os.path.join(HERE, "libgenie.so")
+SHIM_TEST = os.path.join(OBJ, "shim_test")
+
+
+def _cpp_fingerprint():
+    h = hashlib.sha256()
+    files = [os.path.join(CPP, f) for f in sorted(os.listdir(CPP)) if f.endswith((".cc", ".h"))]
+    inc = os.path.join(ROOT, "include")
+    for d, _, fs in sorted(os.walk(inc)):
+        files += [os.path.join(d, f) for f in sorted(fs) if f.endswith(".h")]
+    files.append(os.path.join(ROOT, "tests", "cpp", "shim_test.cc"))
+    for path in files:
+        if os.path.exists(path):
+            with open(path, "rb") as fh:
+                h.update(path.encode() + fh.read())
+    h.update(os.uname().machine.encode())
+    return h.hexdigest()
+
+
+def build_cpp(force=False, verbose=False):
+    """The C++ interface <genie/genie.h> (genie_gb300/cpp, host C++ over the C
+    ABI) as libgenie.so beside libgenie_gb300.so, and its test program."""
+    cxx = shutil.which("g++") or "g++"
+    fp = _cpp_fingerprint()
+    stamp = os.path.join(OBJ, "cpp_fingerprint")
+    if not force and os.path.exists(CPP_LIB) and os.path.exists(SHIM_TEST) and os.path.exists(stamp):
+        with open(stamp) as f:
+            if f.read() == fp:
+                return CPP_LIB
+    os.makedirs(OBJ, exist_ok=True)
+    inc = ["-I" + os.path.join(ROOT, "include")]
+    srcs = [os.path.join(CPP, f) for f in sorted(os.listdir(CPP)) if f.endswith(".cc")]
+    steps = [
+        [cxx, "-std=c++17", "-O2", "-fPIC", "-shared"] + inc + srcs +
+        ["-o", CPP_LIB + ".tmp", "-L" + HERE, "-lgenie_gb300", "-Wl,-rpath,$ORIGIN"],
+    ]
+    for cmd in steps:
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("C++ interface build failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+    os.replace(CPP_LIB + ".tmp", CPP_LIB)
+    cmd = [cxx, "-std=c++17", "-O2"] + inc + [os.path.join(ROOT, "tests", "cpp", "shim_test.cc"), "-o", SHIM_TEST,
+           "-L" + HERE, "-lgenie", "-lgenie_gb300", "-Wl,-rpath,$ORIGIN/.."]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("C++ test build failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+    with open(stamp, "w") as f:
+        f.write(fp)
+    if verbose:
+        print("built", CPP_LIB)
+    return CPP_LIB
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose=True)
+    build_cpp(force="--force" in sys.argv, verbose=True)

@@ -1,0 +1,448 @@
+// genie.cc -- the C++ interface (<genie/genie.h>) over the C ABI
+// (<genie_gb300.h>): configuration, execution policies, table and query
+// objects, CSV/binary I/O and the first/second-level entry points.  Every
+// device operation goes through a genie_* call; status codes become the
+// reference's exception types.
+//
+// Reference behaviour kept (file:line in the reference tree):
+//   Config validation                      interface/config.cc
+//   MakePolicy: single value / single range interface/execution_policy.cc:14-45
+//   BuildTable: dim = width of the first row execution_policy/single_value.cc:10-15
+//   BuildQuery: item j of row i, [v-r, v+r], weight 1, order j
+//                                           original/interface.cc:473-517
+//   CSV tokens split on ',' and blanks      utility/FileReader.cc:54-83
+//   Search = load + build + match           interface/search.cc:11-22
+#include <genie/genie.h>
+
+#include "../../include/genie_gb300.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <sstream>
+
+namespace genie {
+
+// ---------------------------------------------------------------- errors
+
+void exception::throw_on_status(int status) {
+    if (status == GENIE_OK) return;
+    const std::string msg = genie_last_error();
+    switch (status) {
+        case GENIE_ERR_GPU_ALLOC:
+        case GENIE_ERR_ADMISSION:
+            throw gpu_bad_alloc(msg);
+        case GENIE_ERR_NOT_IMPLEMENTED:
+            throw NotImplementedException();
+        case GENIE_ERR_CPU_ALLOC:
+            throw cpu_bad_alloc(msg);
+        case GENIE_ERR_INVALID_ARG:
+        case GENIE_ERR_IO:
+            throw cpu_runtime_error(msg);
+        default:
+            throw gpu_runtime_error(msg);
+    }
+}
+
+using exception::throw_on_status;
+
+// ---------------------------------------------------------------- Config
+
+uint32_t Config::GetK() const { return k_; }
+uint32_t Config::GetQueryRange() const { return query_range_; }
+uint32_t Config::GetNumOfQueries() const { return num_of_queries_; }
+bool Config::GetSaveToGpu() const { return save_to_gpu_; }
+uint8_t Config::GetGpuId() const { return gpu_id_; }
+
+Config &Config::SetK(const uint32_t k) {
+    k_ = k;
+    k_initialized_ = true;
+    return *this;
+}
+Config &Config::SetQueryRange(const uint32_t query_range) {
+    query_range_ = query_range;
+    query_range_initialized_ = true;
+    return *this;
+}
+Config &Config::SetNumOfQueries(const uint32_t num_of_queries) {
+    num_of_queries_ = num_of_queries;
+    num_of_queries_initialized_ = true;
+    return *this;
+}
+Config &Config::SetSaveToGpu(const bool save_to_gpu) {
+    save_to_gpu_ = save_to_gpu;
+    return *this;
+}
+Config &Config::SetGpuId(const uint8_t gpu_id) {
+    gpu_id_ = gpu_id;
+    return *this;
+}
+
+Config &Config::LoadFromFile(const std::string &filename) {
+    std::ifstream in(filename);
+    if (!in) throw exception::cpu_runtime_error("cannot open configuration file " + filename);
+    std::string key;
+    long long v = 0;
+    while (in >> key >> v) {
+        if (key == "k") SetK((uint32_t)v);
+        else if (key == "query_range") SetQueryRange((uint32_t)v);
+        else if (key == "num_of_queries") SetNumOfQueries((uint32_t)v);
+        else if (key == "save_to_gpu") SetSaveToGpu(v != 0);
+        else if (key == "gpu_id") SetGpuId((uint8_t)v);
+        else throw exception::InvalidConfigurationException("unknown configuration key " + key);
+    }
+    return *this;
+}
+
+bool Config::IsKSet() const { return k_initialized_; }
+bool Config::IsQueryRangeSet() const { return query_range_initialized_; }
+bool Config::IsNumOfQueriesSet() const { return num_of_queries_initialized_; }
+
+void Config::Validate() const {
+    if (!k_initialized_) throw exception::InvalidConfigurationException("K is not set.");
+    if (!num_of_queries_initialized_) throw exception::InvalidConfigurationException("Number of query is not set.");
+}
+
+void Config::DisplayConfiguration() {
+    std::cout << "K: " << k_ << "\n"
+              << "Query range: " << (query_range_initialized_ ? std::to_string(query_range_) : "unset") << "\n"
+              << "Number of queries: " << num_of_queries_ << "\n"
+              << "Save to GPU: " << (save_to_gpu_ ? "yes" : "no") << "\n"
+              << "GPU id: " << (int)gpu_id_ << std::endl;
+}
+
+// ---------------------------------------------------------------- inv_table
+
+namespace table {
+
+inv_table::inv_table(const int32_t *values, int64_t n_objects, int32_t n_dims) {
+    throw_on_status(genie_index_create(values, n_objects, n_dims, &ix_));
+}
+inv_table::inv_table(genie_index *adopt) : ix_(adopt) {}
+inv_table::~inv_table() {
+    if (ix_) genie_index_destroy(ix_);
+}
+
+static genie_index_info info_of(genie_index *ix) {
+    genie_index_info inf{};
+    throw_on_status(genie_index_get_info(ix, &inf));
+    return inf;
+}
+
+int inv_table::i_size() const { return (int)info_of(ix_).n_objects; }
+int inv_table::m_size() const { return (int)info_of(ix_).n_dims; }
+int64_t inv_table::inv_size() const { return info_of(ix_).n_ids; }
+
+std::vector<int> inv_table::inv() const {
+    const int64_t n = inv_size();
+    std::vector<uint32_t> ids((size_t)n);
+    throw_on_status(genie_index_copy_out(ix_, ids.data(), nullptr, nullptr, nullptr, nullptr));
+    return std::vector<int>(ids.begin(), ids.end());
+}
+
+void inv_table::save(const std::string &filename) const { throw_on_status(genie_index_save(ix_, filename.c_str())); }
+
+inv_table *inv_table::load(const std::string &filename) {
+    genie_index *ix = nullptr;
+    throw_on_status(genie_index_load(filename.c_str(), &ix));
+    return new inv_table(ix);
+}
+
+}  // namespace table
+
+// ---------------------------------------------------------------- Query
+
+namespace query {
+
+Query::Query(genie::table::inv_table *ref, int index) : ref_(ref), index_(index) {}
+Query::Query(genie::table::inv_table &ref, int index) : ref_(&ref), index_(index) {}
+Query::Query() {}
+
+genie::table::inv_table *Query::ref_table() { return ref_; }
+
+void Query::attr(int index, int low, int up, float weight, int order) { attr(index, low, up, weight, -1.0f, order); }
+
+void Query::attr(int index, int value, float weight, float selectivity, int order) {
+    attr(index, value, value, weight, selectivity, order);
+}
+
+void Query::attr(int index, int low, int up, float weight, float selectivity, int order) {
+    if (!ref_ || index < 0 || index >= ref_->m_size()) return;
+    range r;
+    r.query = index_;
+    r.order = order;
+    r.dim = index;
+    r.low = low;
+    r.up = up;
+    r.weight = weight;
+    r.low_offset = 0;
+    r.up_offset = 0;
+    r.selectivity = selectivity;
+    ranges_.push_back(r);
+}
+
+void Query::clear_dim(int index) {
+    ranges_.erase(std::remove_if(ranges_.begin(), ranges_.end(), [index](const range &r) { return r.dim == index; }),
+                  ranges_.end());
+}
+
+void Query::selectivity(float s) { selectivity_ = s; }
+float Query::selectivity() { return selectivity_; }
+
+void Query::apply_adaptive_query_range() {
+    for (range &r : ranges_) {
+        const float sel = r.selectivity > 0 ? r.selectivity : selectivity_;
+        if (sel <= 0) continue;
+        int32_t lo = r.low, hi = r.up;
+        throw_on_status(genie_index_adaptive_range(ref_->handle(), r.dim, sel, &lo, &hi));
+        r.low = lo;
+        r.up = hi;
+    }
+}
+
+void Query::topk(int k) { topk_ = k; }
+int Query::topk() { return topk_; }
+
+void Query::build() {
+    dims_.clear();
+    for (const range &r : ranges_) {
+        int64_t s = 0, e = 0;
+        throw_on_status(genie_index_item_span(ref_->handle(), r.dim, r.low, r.up, &s, &e));
+        if (e > s) dims_.emplace_back(index_, r.order, (int)s, (int)e, r.weight);
+    }
+}
+
+int Query::dump(std::vector<dim> &vout) {
+    vout.insert(vout.end(), dims_.begin(), dims_.end());
+    return (int)dims_.size();
+}
+
+int Query::dump(std::vector<range> &ranges) {
+    ranges.insert(ranges.end(), ranges_.begin(), ranges_.end());
+    return (int)ranges_.size();
+}
+
+int Query::index() { return index_; }
+int Query::count_ranges() { return (int)ranges_.size(); }
+
+}  // namespace query
+
+// ---------------------------------------------------------------- policies
+
+void ExecutionPolicy::Validate() {
+    if (k_ == 0) throw exception::InvalidConfigurationException("K should be larger than 0.");
+    if (num_of_queries_ == 0) throw exception::InvalidConfigurationException("Number of query should be larger than 0.");
+}
+void ExecutionPolicy::SetK(const uint32_t k) { k_ = k; }
+void ExecutionPolicy::SetNumOfQueries(const uint32_t num_of_queries) { num_of_queries_ = num_of_queries; }
+uint32_t ExecutionPolicy::GetNumOfQueries() const { return num_of_queries_; }
+
+namespace {
+
+// Flattened genie_queries of a query list (arrays owned here).
+struct FlatQueries {
+    std::vector<int64_t> item_off{0};
+    std::vector<int32_t> dim, low, up;
+    std::vector<float> weight;
+    std::vector<uint8_t> weighted;
+    std::vector<uint32_t> k;
+    bool any_weighted = false;
+    int64_t total_k = 0;
+
+    explicit FlatQueries(const std::vector<query::Query> &qs) {
+        for (const query::Query &cq : qs) {
+            query::Query &q = const_cast<query::Query &>(cq);
+            std::vector<query::Query::range> rs;
+            q.dump(rs);
+            for (const auto &r : rs) {
+                dim.push_back(r.dim);
+                low.push_back(r.low);
+                up.push_back(r.up);
+                weight.push_back(r.weight);
+            }
+            item_off.push_back((int64_t)dim.size());
+            weighted.push_back(q.weighted() ? 1 : 0);
+            any_weighted = any_weighted || q.weighted();
+            if (q.topk() <= 0) throw exception::InvalidConfigurationException("a query has no top-k");
+            k.push_back((uint32_t)q.topk());
+            total_k += q.topk();
+        }
+    }
+    genie_queries view() const {
+        genie_queries g{};
+        g.n_queries = (int32_t)k.size();
+        g.item_off = item_off.data();
+        g.dim = dim.data();
+        g.low = low.data();
+        g.up = up.data();
+        g.weight = any_weighted ? weight.data() : nullptr;
+        g.weighted = any_weighted ? weighted.data() : nullptr;
+        g.k = k.data();
+        g.uniform_k = 0;
+        return g;
+    }
+};
+
+SearchResult to_result(const std::vector<uint32_t> &ids, const std::vector<uint32_t> &counts) {
+    return SearchResult(std::vector<int>(ids.begin(), ids.end()), std::vector<int>(counts.begin(), counts.end()));
+}
+
+class MatchPolicy : public ExecutionPolicy {
+  public:
+    explicit MatchPolicy(uint32_t query_range) : query_range_(query_range) {}
+
+    std::shared_ptr<genie::table::inv_table> BuildTable(const genie::TableData &table_data) override {
+        if (table_data.empty()) throw exception::cpu_runtime_error("no data input!");
+        dim_ = (uint32_t)table_data[0].size();
+        std::vector<int32_t> flat;
+        flat.reserve(table_data.size() * dim_);
+        for (const auto &row : table_data) {
+            if (row.size() != dim_) throw exception::cpu_runtime_error("table rows differ in width");
+            flat.insert(flat.end(), row.begin(), row.end());
+        }
+        return std::make_shared<genie::table::inv_table>(flat.data(), (int64_t)table_data.size(), (int32_t)dim_);
+    }
+
+    std::vector<genie::query::Query> BuildQuery(const std::shared_ptr<const genie::table::inv_table> &table,
+                                                const genie::QueryData &query_data) override {
+        genie::table::inv_table *t = const_cast<genie::table::inv_table *>(table.get());
+        const int d = t->m_size();
+        const int r = (int)query_range_;
+        std::vector<genie::query::Query> out;
+        out.reserve(query_data.size());
+        for (size_t i = 0; i < query_data.size(); ++i) {
+            genie::query::Query q(t, (int)i);
+            for (size_t j = 0; j < query_data[i].size() && (int)j < d; ++j) {
+                const int v = query_data[i][j];
+                q.attr((int)j, v - r, v + r, 1.0f, (int)j);
+            }
+            q.topk((int)k_);
+            out.push_back(q);
+        }
+        return out;
+    }
+
+    genie::SearchResult Match(const std::shared_ptr<const genie::table::inv_table> &table,
+                              const std::vector<genie::query::Query> &queries) override {
+        if (queries.empty()) throw exception::cpu_runtime_error("Queries not loaded!");
+        FlatQueries f(queries);
+        const genie_queries g = f.view();
+        std::vector<uint32_t> ids((size_t)std::max<int64_t>(1, f.total_k)), counts(ids.size());
+        throw_on_status(genie_search(table->handle(), &g, ids.data(), counts.data(), nullptr));
+        ids.resize((size_t)f.total_k);
+        counts.resize((size_t)f.total_k);
+        return to_result(ids, counts);
+    }
+
+    genie::SearchResult Match(const std::vector<std::shared_ptr<const genie::table::inv_table> > &tables,
+                              const std::vector<std::vector<genie::query::Query> > &queries) override {
+        if (tables.size() != queries.size()) throw exception::cpu_runtime_error("one query list per table is needed");
+        std::vector<FlatQueries> fs;
+        fs.reserve(queries.size());
+        std::vector<genie_queries> gs;
+        std::vector<genie_index *> ixs;
+        int64_t total = 0;
+        for (size_t t = 0; t < tables.size(); ++t) {
+            fs.emplace_back(queries[t]);
+            total += fs.back().total_k;
+        }
+        for (size_t t = 0; t < tables.size(); ++t) {
+            gs.push_back(fs[t].view());
+            ixs.push_back(tables[t]->handle());
+        }
+        std::vector<uint32_t> ids((size_t)std::max<int64_t>(1, total)), counts(ids.size());
+        throw_on_status(genie_search_multi(ixs.data(), gs.data(), (int32_t)ixs.size(), ids.data(), counts.data(),
+                                           nullptr));
+        ids.resize((size_t)total);
+        counts.resize((size_t)total);
+        return to_result(ids, counts);
+    }
+
+    void Validate() override {
+        ExecutionPolicy::Validate();
+        if (ranged_ && query_range_ == 0)
+            throw exception::InvalidConfigurationException("Query range should be larger than 0.");
+    }
+
+    bool ranged_ = false;
+
+  private:
+    uint32_t query_range_;
+};
+
+}  // namespace
+
+std::shared_ptr<ExecutionPolicy> MakePolicy(const Config &config) {
+    config.Validate();
+    auto p = std::make_shared<MatchPolicy>(config.IsQueryRangeSet() ? config.GetQueryRange() : 0u);
+    p->ranged_ = config.IsQueryRangeSet();
+    p->SetK(config.GetK());
+    p->SetNumOfQueries(config.GetNumOfQueries());
+    p->Validate();
+    throw_on_status(genie_init((int)config.GetGpuId()));
+    return p;
+}
+
+// ---------------------------------------------------------------- I/O
+
+static std::vector<std::vector<int> > read_rows(const std::string &filename, long long limit) {
+    std::vector<std::vector<int> > rows;
+    std::ifstream in(filename);
+    if (!in) return rows;
+    std::string line;
+    while ((limit < 0 || (long long)rows.size() < limit) && std::getline(in, line)) {
+        std::replace(line.begin(), line.end(), ',', ' ');
+        std::istringstream ss(line);
+        std::vector<int> row;
+        long long v;
+        while (ss >> v) row.push_back((int)v);
+        rows.push_back(std::move(row));
+    }
+    return rows;
+}
+
+TableData LoadTableDataFromCsv(const std::string &filename) { return read_rows(filename, -1); }
+
+QueryData LoadQueryDataFromCsv(const std::string &filename, const std::shared_ptr<const ExecutionPolicy> &policy) {
+    return read_rows(filename, (long long)policy->GetNumOfQueries());
+}
+
+std::shared_ptr<genie::table::inv_table> LoadTableFromBinary(const std::string &filename) {
+    return std::shared_ptr<genie::table::inv_table>(genie::table::inv_table::load(filename));
+}
+
+void SaveTableToBinary(const std::string &filename, const std::shared_ptr<const genie::table::inv_table> &table) {
+    table->save(filename);
+}
+
+// ---------------------------------------------------------------- entry points
+
+std::shared_ptr<genie::table::inv_table> BuildTable(std::shared_ptr<genie::ExecutionPolicy> &policy,
+                                                    const TableData &table_data) {
+    return policy->BuildTable(table_data);
+}
+
+std::vector<genie::query::Query> BuildQuery(std::shared_ptr<genie::ExecutionPolicy> &policy,
+                                            const std::shared_ptr<genie::table::inv_table> &table,
+                                            const QueryData &query_data) {
+    return policy->BuildQuery(table, query_data);
+}
+
+SearchResult Match(std::shared_ptr<genie::ExecutionPolicy> &policy,
+                   const std::shared_ptr<genie::table::inv_table> &table,
+                   const std::vector<genie::query::Query> &queries) {
+    return policy->Match(table, queries);
+}
+
+SearchResult Search(std::shared_ptr<genie::ExecutionPolicy> &policy, const std::string &table_filename,
+                    const std::string &query_filename) {
+    TableData table_data = LoadTableDataFromCsv(table_filename);
+    QueryData query_data = LoadQueryDataFromCsv(query_filename, policy);
+    std::shared_ptr<genie::table::inv_table> table = BuildTable(policy, table_data);
+    std::vector<genie::query::Query> queries = BuildQuery(policy, table, query_data);
+    return Match(policy, table, queries);
+}
+
+}  // namespace genie
