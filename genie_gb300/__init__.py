@@ -509,3 +509,4 @@ def Search(policy, table_filename, query_filename):
 
 from .batch import Batch  # noqa: E402
 from .serve import Server, poisson_arrivals  # noqa: E402
+from . import shard  # noqa: E402,F401

@@ -86,6 +86,7 @@ PROTOTYPES = {
     "genie_server_reset_stats": (ctypes.c_int, [P]),
     "genie_server_now_ns": (I64, []),
     "genie_server_destroy": (ctypes.c_int, [P]),
+    "genie_merge_shards": (ctypes.c_int, [I32, P, P, P, P, I32, P, U32, P, P, P]),
     "genie_codec_encode": (I64, [I32, P, I64, P, I64]),
     "genie_codec_encode_bound": (I64, [I64]),
     "genie_codec_decode_device": (ctypes.c_int, [I32, P, P, I64, P, P, P, P]),

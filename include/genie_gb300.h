@@ -285,6 +285,21 @@ int genie_server_reset_stats(genie_server *s);
 int64_t genie_server_now_ns(void);
 int genie_server_destroy(genie_server *s);
 
+/* ---------------------------------------------------------------- shards */
+
+/* Merge the per-shard results of an id-range sharded search: shard s holds
+ * objects [id_offset[s], ...) under local ids and answered the same queries
+ * (k slots per query, layout as genie_search).  Writes the global top-k per
+ * query, sorted (primary desc, id asc), padded (0, 0).  With scores (one
+ * array per shard, or NULL for counts only) the primary is the score; exact
+ * for unweighted queries, and for weighted ones up to scores equal in float.
+ * Host-only.  Replaces the multiload merge (original/interface.cc:114-149)
+ * and the MPI gather + sort of dist_genie (sorting.cc:20-64). */
+int genie_merge_shards(int32_t n_shards, const uint32_t *const *ids, const uint32_t *const *counts,
+                       const float *const *scores, const int64_t *id_offset, int32_t n_queries,
+                       const uint32_t *k, uint32_t uniform_k, uint32_t *out_ids, uint32_t *out_counts,
+                       float *out_scores);
+
 /* ---------------------------------------------------------------- codecs */
 
 /* Host encoder of the reference byte formats (DeviceCodecFactory.cu:13-48).
