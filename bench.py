@@ -47,8 +47,10 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--objects", type=int, default=1_000_000)
-    p.add_argument("--queries", type=int, default=1024)
+    p.add_argument("--workload", default="config1", choices=["config0", "config1", "config2", "config3"],
+                   help="config1 (default) is the headline; the others use the same line format")
+    p.add_argument("--objects", type=int, default=0, help="objects (0: the workload's own size)")
+    p.add_argument("--queries", type=int, default=0, help="queries per batch (0: the workload's own)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--no-serve", action="store_true", help="skip the serving (config 4) leg")
@@ -169,6 +171,45 @@ def max_over_ranks(x, dist, device_is_cuda):
     return float(t.item())
 
 
+WORKLOADS = {
+    "config0": ("config0 plain small: 1,000 objects x 128 dims, uint8 half-normal values with 30% zeros; "
+                "100 queries of 128 exact items from perturbed stored objects; k=10", 1000, 100),
+    "config1": (WORKLOAD, 1_000_000, 1024),
+    "config2": ("config2 compressed: 10,000,000 objects x 32 dims, Zipf(1.1) over 65,536 terms; lists "
+                "in 128-id segments, SERIAL_DELTA_COMP_BP32_VARINT; 4,096 queries x 32 Zipf items; k=32",
+                10_000_000, 4096),
+    "config3": ("config3 batched uneven: 10,000,000 objects x 128 dims uint8 half-normal; 16,384 queries "
+                "of 8-128 items, ranges r in {0,1,2,4}, half weighted U[0.5,2], k in {10,100}",
+                10_000_000, 16384),
+}
+
+
+def gen_workload(args, workloads):
+    """Seeded values and query batch of the workload (host only)."""
+    desc, n0, q0 = WORKLOADS[args.workload]
+    n = args.objects or n0
+    q = args.queries or q0
+    gen = getattr(workloads, args.workload)
+    values, batch = gen(n=n, q=q)
+    return values, batch, desc, n
+
+
+def load_workload(args, g, workloads):
+    """Values, resident table, batch and algorithmic bytes of the workload."""
+    values, batch, desc, n = gen_workload(args, workloads)
+    if args.workload == "config2":
+        table = g.Table.compressed(values, 13, 128)
+    else:
+        table = g.Table.from_values(values)
+    lay = table.layout()
+    offs = lay["key_offsets"]
+    if args.workload == "config2":      # encoded words of the covered segments
+        c = table.compressed_layout()
+        offs = c["seg_word_off"][c["key_seg"]]
+    alg = workloads.algorithmic_bytes(offs, lay["key_base"], lay["dim_min"], lay["dim_max"], batch)
+    return dict(values=values, table=table, batch=batch, alg_bytes=alg, desc=desc, n=n, d=values.shape[1])
+
+
 def serve_leg(g, workloads, t1, b1, args):
     """Config 4 (serving): the config1 index plus config3 and config2 indexes
     (the latter compressed with SERIAL_DELTA_COMP_BP32_VARINT in 128-id
@@ -246,12 +287,11 @@ def run_reference(args, world, rank):
         return
     from genie_gb300 import workloads
     from oracle import oracle
-    values, batch = workloads.config1(n=args.objects, q=args.queries)
+    values, batch, desc, _ = gen_workload(args, workloads)
     ox = oracle.Index(values)
     cores = os.cpu_count() or 1
-    sample_q = min(256, args.queries)
-    sub = dict(item_off=batch["item_off"][:sample_q + 1], dim=batch["dim"], low=batch["low"], up=batch["up"],
-               k=batch["k"][:sample_q])
+    sample_q = min(256, len(batch["k"]))
+    sub = workloads.take_queries(batch, np.arange(sample_q))
     for _ in range(max(1, args.warmup)):
         ox.search(sub, n_threads=cores)
     t0 = time.perf_counter()
@@ -263,9 +303,10 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "step": "%d-query sample of the batch" % sample_q},
+        "config": {"workload": desc, "step": "%d-query sample of the batch" % sample_q},
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": cores, "kind": "port",
-                         "sample": "%d queries of the config1 batch per step, %d steps" % (sample_q, args.steps)},
+                         "sample": "%d queries of the %s batch per step, %d steps" % (sample_q, args.workload,
+                                                                                     args.steps)},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -286,14 +327,13 @@ def main():
     torch.cuda.set_device(local)
     g._check(g.lib().genie_init(local))
 
-    values, batch = workloads.config1(n=args.objects, q=args.queries)
-    table = g.Table.from_values(values)
-    qb = g.QueryBatch(batch["item_off"], batch["dim"], batch["low"], batch["up"], batch["k"])
-    lay = table.layout()
-    alg_bytes = workloads.algorithmic_bytes(lay["key_offsets"], lay["key_base"], lay["dim_min"], lay["dim_max"],
-                                            batch)
+    wl = load_workload(args, g, workloads)
+    values, table, batch, alg_bytes = wl["values"], wl["table"], wl["batch"], wl["alg_bytes"]
+    qb = g.QueryBatch(batch["item_off"], batch["dim"], batch["low"], batch["up"], batch["k"], batch.get("weight"),
+                      batch.get("weighted"))
     n_items = int(batch["item_off"][-1])
     Q = qb.n_queries
+    max_k = int(np.max(batch["k"]))
 
     # one non-default stream carries the L2 flushes, the events and the graph
     # launches (a null handle would select the batch's own stream instead)
@@ -301,12 +341,17 @@ def main():
     torch.cuda.set_stream(stream)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")     # > 2x the 129 MB L2
 
-    bt = g.Batch(table, Q, n_items, 100, use_graph=True)
+    bt = g.Batch(table, Q, n_items, max_k, use_graph=True)
     if args.tuning:
         bt.set_tuning(**{kv.split("=")[0]: int(kv.split("=")[1]) for kv in args.tuning.split(",")})
         tuning = bt.tuning()
-    else:
-        tuning = bt.tuning() if args.no_autotune else bt.autotune(qb)
+    elif args.no_autotune:
+        tuning = bt.tuning()
+    else:       # tune on (at most) the first 1,024 queries
+        sq = min(Q, 1024)
+        sub = workloads.take_queries(batch, np.arange(sq))
+        tuning = bt.autotune(g.QueryBatch(sub["item_off"], sub["dim"], sub["low"], sub["up"], sub["k"],
+                                          sub["weight"], sub["weighted"]))
     bt.stage(qb)
 
     # ---- value: device-resident batch, graph launches, L2 flushed per step
@@ -316,7 +361,7 @@ def main():
     torch.cuda.synchronize()
 
     def load():     # untimed steps of the same batch, so that clock samples see the GPU under load
-        for _ in range(64):
+        for _ in range(4):
             flush.zero_()
             bt.launch(stream.cuda_stream)
         torch.cuda.synchronize()
@@ -346,7 +391,7 @@ def main():
     kernels_per_step = bt.last_stats()[0]
 
     # ---- roofline: per-kernel events (direct launches, same tuning and flushing)
-    bp = g.Batch(table, Q, n_items, 100, use_graph=False)
+    bp = g.Batch(table, Q, n_items, max_k, use_graph=False)
     bp.set_tuning(**{k: v for k, v in tuning.items()})
     bp.stage(qb)
     stage_tot = np.zeros(6)
@@ -357,13 +402,17 @@ def main():
         if i >= args.warmup:
             stage_tot += ms
     names = ["k_plan", "k_bitmap", "k_sparse<packed>", "k_sparse<wide>", "k_dense<u8>", "k_dense<u32>"]
+    # the match kernels that carry the batch (>= 5% of the match time); when
+    # several share it, their posting bytes are counted over their summed time
+    match_ms = stage_tot[1:]
+    busy = [i + 1 for i in range(len(match_ms)) if match_ms[i] >= 0.05 * match_ms.sum()]
     dom = int(np.argmax(stage_tot[1:]) + 1)
-    dom_ms = stage_tot[dom] / args.steps
+    dom_ms = float(sum(stage_tot[i] for i in busy)) / args.steps
     peak, peak_kind = peaks()
     achieved = alg_bytes / (dom_ms / 1e3) / 1e9
-    traffic = ncu_traffic(names[dom])
+    traffic = ncu_traffic(names[dom]) if len(busy) == 1 else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": names[dom], "kernel_ms": dom_ms,
+                "traffic": traffic, "kernel": "+".join(names[i] for i in busy), "kernel_ms": dom_ms,
                 "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind,
                 "stage_ms": {n: float(v / args.steps) for n, v in zip(names, stage_tot)}}
 
@@ -395,7 +444,9 @@ def main():
     plain = world * Q * args.steps / max_over_ranks(sum(plain_times), dist, True)
     same = bool(np.array_equal(pid, ids_graph) and np.array_equal(pcnt, cnt_graph))
 
-    # ---- CPU baseline: the oracle on this host's cores (rank 0)
+    # ---- CPU baseline: the oracle on this host's cores (rank 0), over the
+    # whole batch repeated, or over its first queries in growing samples when
+    # the whole batch would take longer than --cpu-seconds
     cpu = None
     if rank == 0:
         from oracle import oracle
@@ -403,19 +454,29 @@ def main():
         t_build = time.perf_counter()
         ox = oracle.Index(values)
         t_build = time.perf_counter() - t_build
-        reps, t_cpu = 0, 0.0
-        while reps < 1 or t_cpu < args.cpu_seconds:
+        sq = min(Q, 64)
+        while True:
+            sub = workloads.take_queries(batch, np.arange(sq))
             t0 = time.perf_counter()
-            oid, ocnt, _, _ = ox.search(qb.as_oracle_batch(), n_threads=cores)
+            oid, ocnt, _, _ = ox.search(sub, n_threads=cores)
+            dt = time.perf_counter() - t0
+            if sq == Q or dt * 2 > args.cpu_seconds:
+                break
+            sq = min(Q, sq * 4)
+        reps, t_cpu = 1, dt
+        while sq == Q and t_cpu < args.cpu_seconds:
+            t0 = time.perf_counter()
+            ox.search(sub, n_threads=cores)
             t_cpu += time.perf_counter() - t0
             reps += 1
-        cpu = {"value": Q * reps / t_cpu, "unit": "queries/s", "cores": cores, "kind": "port",
-               "sample": "the full %d-query batch x %d repetitions (oracle index build %.1f s, untimed)"
-                         % (Q, reps, t_build),
-               "matches_gpu": bool(np.array_equal(oid, ids_graph) and np.array_equal(ocnt, cnt_graph))}
+        nk = int(sub["k"].sum())
+        cpu = {"value": sq * reps / t_cpu, "unit": "queries/s", "cores": cores, "kind": "port",
+               "sample": "the first %d of the %d queries x %d repetitions (oracle index build %.1f s, untimed)"
+                         % (sq, Q, reps, t_build),
+               "matches_gpu": bool(np.array_equal(oid, ids_graph[:nk]) and np.array_equal(ocnt, cnt_graph[:nk]))}
 
     serving = None
-    if rank == 0 and not args.no_serve:
+    if rank == 0 and not args.no_serve and args.workload == "config1":
         serving = serve_leg(g, workloads, table, batch, args)
 
     if rank == 0:
@@ -423,8 +484,10 @@ def main():
             "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic (seeded generator with the config1 shapes and distributions)",
-            "config": {"workload": WORKLOAD, "n_objects": args.objects, "n_dims": 240, "n_queries": Q, "k": 100,
+            "data": "synthetic (seeded generator with the %s shapes and distributions)" % args.workload,
+            "config": {"workload": wl["desc"], "n_objects": wl["n"], "n_dims": wl["d"], "n_queries": Q,
+                       "k": max_k if int(np.min(batch["k"])) == max_k else "per query (%d..%d)" % (
+                           int(np.min(batch["k"])), max_k),
                        "l2": "flushed by a 512 MiB device write before every timed step",
                        "tuning": tuning, "parallelism": "replica per GPU" if world > 1 else "single GPU"},
             "e2e": {"value": e2e, "unit": "queries/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
