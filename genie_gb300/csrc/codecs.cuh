@@ -30,7 +30,7 @@ namespace gg {
 // sequence positions are base + before(l) + 0..cnt-1 (before = exclusive
 // prefix of cnt over lanes).  The emitter applies the delta stages in
 // sequence order and hands each value to `visit`.
-template <class V>
+template <class V, bool POS = true>
 struct Emitter {
     int deltas;
     uint32_t carry1 = 0, carry2 = 0;
@@ -38,10 +38,14 @@ struct Emitter {
     V &visit;
     __device__ Emitter(int d, V &v) : deltas(d), visit(v) {}
     __device__ __forceinline__ void emit(const uint32_t *val, int cnt) {
-        // sequence position of this lane's first value
-        const uint32_t cincl = warp_incl_scan((uint32_t)cnt);
-        const uint32_t pos0 = emitted + cincl - (uint32_t)cnt;
-        emitted += __shfl_sync(0xffffffffu, cincl, 31);
+        // sequence position of this lane's first value (skipped when the
+        // visitor does not use positions)
+        uint32_t pos0 = 0;
+        if (POS) {
+            const uint32_t cincl = warp_incl_scan((uint32_t)cnt);
+            pos0 = emitted + cincl - (uint32_t)cnt;
+            emitted += __shfl_sync(0xffffffffu, cincl, 31);
+        }
         // stage 1: inclusive running sum within the lane, then across lanes
         uint32_t loc[4];
         uint32_t s = 0;
@@ -84,25 +88,49 @@ struct Emitter {
     }
 };
 
+// Word sources of the decoders.  Every lane of the warp calls word() the
+// same number of times (the register source shuffles).
+struct GlobalWords {      // words read from global memory
+    const uint32_t *__restrict__ w;
+    __device__ __forceinline__ uint32_t word(int64_t i) const { return __ldg(w + i); }
+    // word i where cond holds, else 0 (read only where cond holds)
+    __device__ __forceinline__ uint32_t word_if(int64_t i, bool cond) const { return cond ? __ldg(w + i) : 0u; }
+};
+struct RegWords {         // a segment of <= 64 words held two per lane
+    int64_t base;
+    uint32_t r0, r1;
+    __device__ __forceinline__ uint32_t word(int64_t i) const {
+        const uint32_t rel = (uint32_t)(i - base);
+        const uint32_t a = __shfl_sync(0xffffffffu, r0, rel & 31u);
+        const uint32_t b = __shfl_sync(0xffffffffu, r1, rel & 31u);
+        return rel < 32u ? a : (rel < 64u ? b : 0u);
+    }
+    __device__ __forceinline__ uint32_t word_if(int64_t i, bool cond) const {
+        const uint32_t x = word(i);      // every lane shuffles
+        return cond ? x : 0u;
+    }
+};
+
 // Words [w0, w1) as values, 32 per step.
-template <class E>
-__device__ __forceinline__ void dec_copy(const uint32_t *__restrict__ w, int64_t w0, int64_t w1, E &em) {
+template <class S, class E>
+__device__ __forceinline__ void dec_copy(const S &src, int64_t w0, int64_t w1, E &em) {
     for (int64_t b = w0; b < w1; b += 32) {
         int64_t i = b + lane_id();
-        uint32_t v[1] = {i < w1 ? __ldg(w + i) : 0u};
+        const uint32_t x = src.word(i < w1 ? i : w0);
+        uint32_t v[1] = {i < w1 ? x : 0u};
         em.emit(v, i < w1 ? 1 : 0);
     }
 }
 
 // One BP32 stream starting at word w0 ([n][blocks...]); returns the word
 // after it.
-template <class E>
-__device__ __forceinline__ int64_t dec_bp32(const uint32_t *__restrict__ w, int64_t w0, E &em) {
+template <class S, class E>
+__device__ __forceinline__ int64_t dec_bp32(const S &src, int64_t w0, E &em) {
     const uint32_t lane = lane_id();
-    const uint32_t n = __ldg(w + w0);
+    const uint32_t n = src.word(w0);
     int64_t p = w0 + 1;
     for (uint32_t done = 0; done < n; done += 128) {
-        const uint32_t hdr = __ldg(w + p);
+        const uint32_t hdr = src.word(p);
         const uint32_t rem = n - done;
         const uint32_t howmany = rem >= 128 ? 4u : (rem + 31) / 32;
         int64_t off = p + 1;
@@ -111,11 +139,11 @@ __device__ __forceinline__ int64_t dec_bp32(const uint32_t *__restrict__ w, int6
             const uint32_t idx = done + mb * 32 + lane;
             uint32_t v = 0;
             if (b == 32) {
-                v = __ldg(w + off + lane);
-            } else if (b > 0) {
+                v = src.word(off + lane);
+            } else if (b > 0) {         // b is warp-uniform: every lane reads two words
                 const uint32_t bit = lane * b, wi = bit >> 5, sh = bit & 31;
-                const uint32_t lo = __ldg(w + off + wi);
-                const uint32_t hi = (sh + b > 32) ? __ldg(w + off + wi + 1) : 0u;
+                const uint32_t lo = src.word(off + wi);
+                const uint32_t hi = src.word_if(off + wi + 1, sh + b > 32);
                 v = (uint32_t)((((uint64_t)hi << 32) | lo) >> sh) & ((1u << b) - 1u);
             }
             uint32_t vv[1] = {v};
@@ -130,14 +158,15 @@ __device__ __forceinline__ int64_t dec_bp32(const uint32_t *__restrict__ w, int6
 // Varint bytes of words [w0, w1): a lane owns one word; each byte with bit 7
 // set ends a value of at most five bytes, so a value spans at most this word
 // and the previous one.
-template <class E>
-__device__ __forceinline__ void dec_varint(const uint32_t *__restrict__ w, int64_t w0, int64_t w1, E &em) {
+template <class S, class E>
+__device__ __forceinline__ void dec_varint(const S &src, int64_t w0, int64_t w1, E &em) {
     const uint32_t lane = lane_id();
     uint32_t prev_last = 0;            // previous chunk's last word
     bool have_prev = false;
     for (int64_t b = w0; b < w1; b += 32) {
         const int64_t i = b + lane;
-        const uint32_t cur = i < w1 ? __ldg(w + i) : 0u;
+        const uint32_t raw = src.word(i < w1 ? i : w0);
+        const uint32_t cur = i < w1 ? raw : 0u;
         uint32_t prv = __shfl_up_sync(0xffffffffu, cur, 1);
         if (lane == 0) prv = have_prev ? prev_last : 0u;
         const bool prv_valid = lane > 0 || have_prev;
@@ -168,33 +197,63 @@ __device__ __forceinline__ void dec_varint(const uint32_t *__restrict__ w, int64
     }
 }
 
-// Decode one encoded segment (words [w0, w1)) and visit its values in order.
+// Decode one encoded segment (words [w0, w1)) from a word source and visit
+// its values in order.
+template <bool POS, class S, class V>
+__device__ __forceinline__ void decode_words(int codec, const S &src, int64_t w0, int64_t w1, V &visit) {
+    int deltas, inner;
+    codec_parts(codec, deltas, inner);
+    Emitter<V, POS> em(deltas, visit);
+    switch (inner) {
+    case kInnerCopy:
+        dec_copy(src, w0, w1, em);
+        break;
+    case kInnerBP32:
+        dec_bp32(src, w0, em);
+        break;
+    case kInnerVarint:
+        dec_varint(src, w0, w1, em);
+        break;
+    default: {     // composite: [len1][BP32 (len1 words)][tail]
+        const uint32_t len1 = src.word(w0);
+        int64_t p = w0 + 1;
+        if (len1) dec_bp32(src, p, em);
+        p += len1;
+        if (p < w1) {
+            if (inner == kInnerCompCopy) dec_copy(src, p, w1, em);
+            else dec_varint(src, p, w1, em);
+        }
+    }
+    }
+}
+
+// Decode one encoded segment and visit (value, sequence position) in order.
+// A segment of at most 64 words is read in one coalesced step and decoded
+// from registers; a longer one is read word by word.
 template <class V>
 __device__ __forceinline__ void decode_segment(int codec, const uint32_t *__restrict__ w, int64_t w0, int64_t w1,
                                                V &visit) {
-    int deltas, inner;
-    codec_parts(codec, deltas, inner);
-    Emitter<V> em(deltas, visit);
-    switch (inner) {
-    case kInnerCopy:
-        dec_copy(w, w0, w1, em);
-        break;
-    case kInnerBP32:
-        dec_bp32(w, w0, em);
-        break;
-    case kInnerVarint:
-        dec_varint(w, w0, w1, em);
-        break;
-    default: {     // composite: [len1][BP32 (len1 words)][tail]
-        const uint32_t len1 = __ldg(w + w0);
-        int64_t p = w0 + 1;
-        if (len1) dec_bp32(w, p, em);
-        p += len1;
-        if (p < w1) {
-            if (inner == kInnerCompCopy) dec_copy(w, p, w1, em);
-            else dec_varint(w, p, w1, em);
-        }
+    if (w1 - w0 <= 64) {
+        const uint32_t lane = lane_id();
+        RegWords src{w0, w0 + lane < w1 ? __ldg(w + w0 + lane) : 0u,
+                     w0 + 32 + lane < w1 ? __ldg(w + w0 + 32 + lane) : 0u};
+        decode_words<true>(codec, src, w0, w1, visit);
+    } else {
+        decode_words<true>(codec, GlobalWords{w}, w0, w1, visit);
     }
+}
+
+// The same for a visitor of values only (no sequence positions).
+template <class V>
+__device__ __forceinline__ void decode_segment_values(int codec, const uint32_t *__restrict__ w, int64_t w0,
+                                                      int64_t w1, V &visit) {
+    if (w1 - w0 <= 64) {
+        const uint32_t lane = lane_id();
+        RegWords src{w0, w0 + lane < w1 ? __ldg(w + w0 + lane) : 0u,
+                     w0 + 32 + lane < w1 ? __ldg(w + w0 + 32 + lane) : 0u};
+        decode_words<false>(codec, src, w0, w1, visit);
+    } else {
+        decode_words<false>(codec, GlobalWords{w}, w0, w1, visit);
     }
 }
 

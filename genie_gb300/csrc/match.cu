@@ -425,7 +425,7 @@ __device__ __forceinline__ void stream_segments(const DevIndex &ix, const ItemSt
         auto v = [&](uint32_t id, uint32_t) {
             if (id >= lo && id < hi && inc) visit(id, inc);
         };
-        decode_segment(ix.codec, ix.words, ix.seg_word_off[seg], ix.seg_word_off[seg + 1], v);
+        decode_segment_values(ix.codec, ix.words, ix.seg_word_off[seg], ix.seg_word_off[seg + 1], v);
     }
 }
 
