@@ -123,7 +123,8 @@ __device__ __forceinline__ void dec_copy(const S &src, int64_t w0, int64_t w1, E
 }
 
 // One BP32 stream starting at word w0 ([n][blocks...]); returns the word
-// after it.
+// after it.  Lane l decodes values 4l..4l+3 of each 128-value block (all in
+// miniblock l/8), so one emit (one prefix scan) covers the whole block.
 template <class S, class E>
 __device__ __forceinline__ int64_t dec_bp32(const S &src, int64_t w0, E &em) {
     const uint32_t lane = lane_id();
@@ -133,24 +134,32 @@ __device__ __forceinline__ int64_t dec_bp32(const S &src, int64_t w0, E &em) {
         const uint32_t hdr = src.word(p);
         const uint32_t rem = n - done;
         const uint32_t howmany = rem >= 128 ? 4u : (rem + 31) / 32;
-        int64_t off = p + 1;
-        for (uint32_t mb = 0; mb < howmany; ++mb) {
-            const uint32_t b = (hdr >> (24 - 8 * mb)) & 255u;
-            const uint32_t idx = done + mb * 32 + lane;
-            uint32_t v = 0;
-            if (b == 32) {
-                v = src.word(off + lane);
-            } else if (b > 0) {         // b is warp-uniform: every lane reads two words
-                const uint32_t bit = lane * b, wi = bit >> 5, sh = bit & 31;
-                const uint32_t lo = src.word(off + wi);
-                const uint32_t hi = src.word_if(off + wi + 1, sh + b > 32);
-                v = (uint32_t)((((uint64_t)hi << 32) | lo) >> sh) & ((1u << b) - 1u);
+        // widths of the miniblocks present (a short tail packs fewer)
+        uint32_t bw[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) bw[m] = (uint32_t)m < howmany ? (hdr >> (24 - 8 * m)) & 255u : 0u;
+        const uint32_t mb = lane >> 3;
+        uint32_t b = bw[0], before = 0;
+#pragma unroll
+        for (int m = 1; m < 4; ++m)
+            if ((uint32_t)m <= mb) {
+                before += bw[m - 1];
+                b = bw[m];
             }
-            uint32_t vv[1] = {v};
-            em.emit(vv, idx < n ? 1 : 0);
-            off += b;
+        const int64_t off = p + 1 + before;
+        const uint32_t j0 = (lane & 7u) * 4u;
+        const uint32_t mask = b >= 32 ? 0xFFFFFFFFu : (1u << b) - 1u;
+        uint32_t v[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t bit = (j0 + k) * b, wi = bit >> 5, sh = bit & 31;
+            const uint32_t lo = src.word_if(off + wi, b > 0);
+            const uint32_t hi = src.word_if(off + wi + 1, b > 0 && sh + b > 32);
+            v[k] = (uint32_t)((((uint64_t)hi << 32) | lo) >> sh) & mask;
         }
-        p = off;
+        const int have = (int)min(4u, rem > 4 * lane ? rem - 4 * lane : 0u);
+        em.emit(v, have);
+        p += 1 + bw[0] + bw[1] + bw[2] + bw[3];
     }
     return p;
 }
