@@ -86,13 +86,18 @@ class Table:
         self._h = ctypes.c_void_p(handle)
         self._info = None
 
+    BUILDERS = {"auto": 0, "host": 1, "device": 2}
+
     @classmethod
-    def from_values(cls, values):
+    def from_values(cls, values, builder="auto"):
+        """builder: "auto" (on the device when every dim spans <= 16384
+        values, else on the host), "host" or "device"."""
         values = np.ascontiguousarray(values, dtype=np.int32)
         if values.ndim != 2 or values.size == 0:
             raise cpu_runtime_error("no data input!")
         h = ctypes.c_void_p()
-        _check(lib().genie_index_create(values.ctypes.data, values.shape[0], values.shape[1], ctypes.byref(h)))
+        _check(lib().genie_index_create_with(values.ctypes.data, values.shape[0], values.shape[1],
+                                             cls.BUILDERS[builder], ctypes.byref(h)))
         return cls(h.value)
 
     @classmethod
@@ -155,6 +160,13 @@ class Table:
         _check(lib().genie_index_copy_out(self._h, None, ko.ctypes.data, kb.ctypes.data, mn.ctypes.data,
                                           mx.ctypes.data))
         return dict(key_offsets=ko, key_base=kb, dim_min=mn, dim_max=mx)
+
+    def ids(self):
+        """The device posting array (ids ordered by (dim, value, id))."""
+        inf = self.info()
+        out = np.zeros(max(1, inf.n_ids), np.uint32)
+        _check(lib().genie_index_copy_out(self._h, out.ctypes.data, None, None, None, None))
+        return out[: inf.n_ids]
 
     def compressed_layout(self):
         inf = self.info()

@@ -52,6 +52,7 @@ PROTOTYPES = {
     "genie_version": (ctypes.c_int, []),
     "genie_init": (ctypes.c_int, [ctypes.c_int]),
     "genie_index_create": (ctypes.c_int, [P, I64, I32, P]),
+    "genie_index_create_with": (ctypes.c_int, [P, I64, I32, I32, P]),
     "genie_index_create_bag": (ctypes.c_int, [P, P, I64, P]),
     "genie_index_create_compressed": (ctypes.c_int, [P, I64, I32, I32, I32, P]),
     "genie_index_destroy": (ctypes.c_int, [P]),

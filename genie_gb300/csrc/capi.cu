@@ -199,17 +199,19 @@ int check_device_error(uint32_t err) {
 }
 
 // Upload a host CSR and fill the device view.
-int upload_index(genie_index *ix) {
+int upload_index(genie_index *ix, int64_t device_ids) {
     const HostIndex &h = ix->host;
     cudaError_t e;
-    const size_t ids_bytes = h.ids.size() * 4 + 64;     // padded for vector loads
-    if ((e = ix->d_ids.reserve(ids_bytes))) return cuda_fail(e, "index ids");
-    if ((e = cudaMemset(ix->d_ids.p, 0, ids_bytes))) return cuda_fail(e, "index ids");
-    if (!h.ids.empty() && (e = cudaMemcpy(ix->d_ids.p, h.ids.data(), h.ids.size() * 4, cudaMemcpyHostToDevice)))
-        return cuda_fail(e, "index ids upload");
-    if ((e = ix->d_key_off.reserve(h.key_off.size() * 8))) return cuda_fail(e, "key offsets");
-    if ((e = cudaMemcpy(ix->d_key_off.p, h.key_off.data(), h.key_off.size() * 8, cudaMemcpyHostToDevice)))
-        return cuda_fail(e, "key offsets upload");
+    if (device_ids < 0) {       // ids and key offsets come from the host mirror
+        const size_t ids_bytes = h.ids.size() * 4 + 64;     // padded for vector loads
+        if ((e = ix->d_ids.reserve(ids_bytes))) return cuda_fail(e, "index ids");
+        if ((e = cudaMemset(ix->d_ids.p, 0, ids_bytes))) return cuda_fail(e, "index ids");
+        if (!h.ids.empty() && (e = cudaMemcpy(ix->d_ids.p, h.ids.data(), h.ids.size() * 4, cudaMemcpyHostToDevice)))
+            return cuda_fail(e, "index ids upload");
+        if ((e = ix->d_key_off.reserve(h.key_off.size() * 8))) return cuda_fail(e, "key offsets");
+        if ((e = cudaMemcpy(ix->d_key_off.p, h.key_off.data(), h.key_off.size() * 8, cudaMemcpyHostToDevice)))
+            return cuda_fail(e, "key offsets upload");
+    }
     if ((e = ix->d_key_base.reserve(h.key_base.size() * 8))) return cuda_fail(e, "key base");
     if ((e = cudaMemcpy(ix->d_key_base.p, h.key_base.data(), h.key_base.size() * 8, cudaMemcpyHostToDevice)))
         return cuda_fail(e, "key base upload");
@@ -219,7 +221,7 @@ int upload_index(genie_index *ix) {
     if ((e = ix->d_dim_max.reserve(h.dim_max.size() * 4))) return cuda_fail(e, "dim max");
     if ((e = cudaMemcpy(ix->d_dim_max.p, h.dim_max.data(), h.dim_max.size() * 4, cudaMemcpyHostToDevice)))
         return cuda_fail(e, "dim max upload");
-    ix->n_ids = (int64_t)h.ids.size();
+    ix->n_ids = device_ids < 0 ? (int64_t)h.ids.size() : device_ids;
     DevIndex &d = ix->dev;
     memset(&d, 0, sizeof(d));
     d.ids = (const uint32_t *)ix->d_ids.p;
@@ -235,8 +237,8 @@ int upload_index(genie_index *ix) {
     return GENIE_OK;
 }
 
-int finish_index_create(genie_index *ix, genie_index **out) {
-    int rc = upload_index(ix);
+int finish_index_create(genie_index *ix, genie_index **out, int64_t device_ids) {
+    int rc = upload_index(ix, device_ids);
     if (rc) {
         delete ix;
         return rc;
@@ -350,11 +352,31 @@ static genie_index *new_index() {
 }
 
 int genie_index_create(const int32_t *values, int64_t n_objects, int32_t n_dims, genie_index **out) {
+    return genie_index_create_with(values, n_objects, n_dims, GENIE_BUILD_AUTO, out);
+}
+
+int genie_index_create_with(const int32_t *values, int64_t n_objects, int32_t n_dims, int32_t where,
+                            genie_index **out) {
     if (!out) return fail(GENIE_ERR_INVALID_ARG, "out is NULL");
     *out = nullptr;
     if (!values || n_objects <= 0 || n_dims <= 0) return fail(GENIE_ERR_INVALID_ARG, "no data input");
+    if (where < GENIE_BUILD_AUTO || where > GENIE_BUILD_DEVICE) return fail(GENIE_ERR_INVALID_ARG, "unknown builder");
+    if (n_objects > (int64_t)UINT32_MAX) return fail(GENIE_ERR_INVALID_ARG, "index build failed (N must be < 2^32)");
     genie_index *ix = new_index();
     if (!ix) return cuda_fail(device_context(0).prepare_error, "kernel setup");
+    if (where != GENIE_BUILD_HOST) {
+        bool used = false;
+        const int rc = build_device_index(values, n_objects, n_dims, ix, &used);
+        if (rc) {
+            delete ix;
+            return rc;
+        }
+        if (used) return finish_index_create(ix, out, n_objects * (int64_t)n_dims);
+        if (where == GENIE_BUILD_DEVICE) {
+            delete ix;
+            return fail(GENIE_ERR_NOT_IMPLEMENTED, "device build: a dim spans more than 16384 values");
+        }
+    }
     if (!build_host_index(values, n_objects, n_dims, ix->host)) {
         delete ix;
         return fail(GENIE_ERR_INVALID_ARG, "index build failed (N must be < 2^32)");

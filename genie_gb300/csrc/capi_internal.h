@@ -59,6 +59,16 @@ int64_t count_units(const HostIndex &h, const genie_queries *q);
 
 }  // namespace gg
 
+namespace gg {
+// Device arrays and view of an index from its host mirror; with device_ids
+// >= 0 the ids and key offsets are on the device already (device build).
+int upload_index(genie_index *ix, int64_t device_ids = -1);
+int finish_index_create(genie_index *ix, genie_index **out, int64_t device_ids = -1);
+// Device build of a one-value-per-object index (build_index.cu); *used is
+// false when a dim's value range needs the host builder.
+int build_device_index(const int32_t *values, int64_t n, int32_t d, genie_index *ix, bool *used);
+}  // namespace gg
+
 struct genie_index {
     int device = 0;
     bool is_bag = false;

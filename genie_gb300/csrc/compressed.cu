@@ -15,8 +15,6 @@
 
 namespace gg {
 
-int upload_index(genie_index *ix);
-
 int upload_compressed(genie_index *ix, const std::vector<uint32_t> &words, const std::vector<int64_t> &key_seg,
                       const std::vector<int64_t> &seg_word_off, const std::vector<uint32_t> &seg_first,
                       const std::vector<uint32_t> &seg_len) {

@@ -84,6 +84,17 @@ typedef struct {
 int genie_index_create(const int32_t *values, int64_t n_objects, int32_t n_dims,
                        genie_index **out);
 
+/* Where genie_index_create_with builds the CSR: the device (a stable
+ * counting sort per dim, for dims of at most 16384 distinct values) with the
+ * host as fallback, the host only, or the device only. */
+enum genie_builder { GENIE_BUILD_AUTO = 0, GENIE_BUILD_HOST = 1, GENIE_BUILD_DEVICE = 2 };
+/* genie_index_create with a choice of builder; every builder gives the same
+ * index.  GENIE_BUILD_DEVICE fails with GENIE_ERR_NOT_IMPLEMENTED when a dim's
+ * range is too wide for it.  Replaces the host-side inv_list::invert +
+ * inv_table::build (table/inv_list.cc:295-320, table/inv_table.cu:267-350). */
+int genie_index_create_with(const int32_t *values, int64_t n_objects, int32_t n_dims, int32_t where,
+                            genie_index **out);
+
 /* Single-dim "bag" index (every value of row r lists r).  Replaces
  * load_table_bijectMap (original/interface.cc:621-646, inv_list.cc:51-84). */
 int genie_index_create_bag(const int32_t *values, const int64_t *row_off,
