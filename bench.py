@@ -402,10 +402,10 @@ def main():
         if i >= args.warmup:
             stage_tot += ms
     names = ["k_plan", "k_bitmap", "k_sparse<packed>", "k_sparse<wide>", "k_dense<u8>", "k_dense<u32>"]
-    # the match kernels that carry the batch (>= 5% of the match time); when
+    # the match kernels that carry the batch (>= 15% of the match time); when
     # several share it, their posting bytes are counted over their summed time
     match_ms = stage_tot[1:]
-    busy = [i + 1 for i in range(len(match_ms)) if match_ms[i] >= 0.05 * match_ms.sum()]
+    busy = [i + 1 for i in range(len(match_ms)) if match_ms[i] >= 0.15 * match_ms.sum()]
     dom = int(np.argmax(stage_tot[1:]) + 1)
     dom_ms = float(sum(stage_tot[i] for i in busy)) / args.steps
     peak, peak_kind = peaks()

@@ -40,7 +40,7 @@ constexpr int kBmRound = 16;              // chunk loads in flight per lane
 
 // Byte offsets of the shared-memory regions (host and device agree).
 struct BmLayout {
-    uint32_t bm, mt, mlist, cstart, ccnt, ss, bytes, bm_words;
+    uint32_t bm, mt, mlist, chunk, ss, bytes, bm_words;
 };
 __host__ __device__ inline uint32_t bm_align(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
 __host__ __device__ inline BmLayout bm_layout(int64_t n_objects, uint32_t mslots) {
@@ -50,8 +50,7 @@ __host__ __device__ inline BmLayout bm_layout(int64_t n_objects, uint32_t mslots
     L.bm = o;     o += bm_align(L.bm_words * 4, 128);
     L.mt = o;     o += bm_align(mslots * 4, 128);
     L.mlist = o;  o += bm_align(mslots / 2 * 4, 128);     // slots of the table's entries
-    L.cstart = o; o += kBmChunks * 8;      // also the candidate keys after streaming
-    L.ccnt = o;   o += kBmChunks;
+    L.chunk = o;  o += kBmChunks * 8;      // also the candidate keys after streaming
     L.ss = o;     o += bm_align((uint32_t)sizeof(SelectScratch), 16);
     L.bytes = bm_align(o, 128);
     return L;
@@ -135,10 +134,10 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
     const BmLayout L = bm_layout(ix.n_objects, mslots);
     uint32_t *bm = (uint32_t *)(smem + L.bm);
     uint32_t *mt = (uint32_t *)(smem + L.mt);
-    int64_t *cstart = (int64_t *)(smem + L.cstart);
-    uint8_t *ccnt = smem + L.ccnt;
+    // chunk entry: posting position of its first id << 6 | ids in it (1..32)
+    uint64_t *chunk = (uint64_t *)(smem + L.chunk);
     uint32_t *mlist = (uint32_t *)(smem + L.mlist);
-    uint64_t *cand = (uint64_t *)(smem + L.cstart);                  // [0, kCandCap)
+    uint64_t *cand = (uint64_t *)(smem + L.chunk);                  // [0, kCandCap)
     uint32_t *tie_ids = (uint32_t *)(cand + kCandCap);               // [0, kCandCap)
     uint64_t *tie_keys = cand + kCandCap + kCandCap / 2;             // [0, kCandCap / 2)
     SelectScratch &ss = *(SelectScratch *)(smem + L.ss);
@@ -200,10 +199,13 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
         uint32_t n_chunks = 0;
         const uint32_t c0 = block_excl_scan(nch, ss.tmp, &n_chunks);     // ends with a barrier
         const BmQuery d = s_qd[it & 1];
-        for (uint32_t c = 0; c < nch && c0 + c < kBmChunks; ++c) {
-            cstart[c0 + c] = sp_start + 32 * (int64_t)c;
-            ccnt[c0 + c] = (uint8_t)min((int64_t)32, sp_len - 32 * (int64_t)c);
-        }
+        for (uint32_t c = 0; c < nch && c0 + c < kBmChunks; ++c)
+            chunk[c0 + c] = ((uint64_t)(sp_start + 32 * (int64_t)c) << 6) |
+                            (uint64_t)min((int64_t)32, sp_len - 32 * (int64_t)c);
+        // empty entries up to whole rounds of every warp, so rounds need no bounds
+        const uint32_t round_ids = 32u * kBmRound;
+        const uint32_t padded = min(kBmChunks, (n_chunks + round_ids - 1) / round_ids * round_ids);
+        for (uint32_t c = n_chunks + tid; c < padded; c += kBmThreads) chunk[c] = 0ull;
         // spans of the next query, in flight during this one
         sp_start = 0;
         sp_len = 0;
@@ -250,12 +252,9 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
             uint32_t v[kBmRound], ok = 0;
 #pragma unroll
             for (int r = 0; r < kBmRound; ++r) {
-                const uint32_t c = j0 + r * 32;
-                const bool inb = c < nc;
-                const int64_t st = inb ? cstart[c] : 0;
-                const uint32_t n = inb ? ccnt[c] : 0u;
-                const bool g = lane < n;
-                v[r] = __ldg(ix.ids + (g ? st + lane : 0));
+                const uint64_t e = chunk[j0 + r * 32];
+                const bool g = lane < (uint32_t)(e & 63u);
+                v[r] = __ldg(ix.ids + (g ? (int64_t)(e >> 6) + lane : 0));
                 ok |= (g ? 1u : 0u) << r;
             }
             uint32_t old[kBmRound];

@@ -77,7 +77,6 @@ cudaError_t Workspace::reserve(int64_t Q, int64_t items, int64_t units, int64_t 
     RES(item_k0, items * 8 + 16);
     RES(item_nk, items * 4 + 16);
     RES(item_inc, items * 4 + 16);
-    RES(q_unit_off, (Q + 1) * 8 + 16);
     RES(span_start, units * 8 + 16);
     RES(span_len, units * 8 + 16);
     RES(inc, units * 4 + 16);
@@ -102,7 +101,7 @@ cudaError_t Workspace::reserve(int64_t Q, int64_t items, int64_t units, int64_t 
 
 void Workspace::release() {
     DevBuf *all[] = {&item_off, &dim, &low, &up, &weight, &weighted, &k, &out_off, &item_k0, &item_nk,
-                     &item_inc, &q_unit_off, &span_start,
+                     &item_inc, &span_start,
                      &span_len, &inc, &qinfo, &work, &ctr, &qstate, &done, &part_cnt, &scratch,
                      &out_ids, &out_counts, &out_scores};
     for (DevBuf *b : all) b->release();
@@ -113,7 +112,6 @@ Work Workspace::view(int64_t Q, bool scores) const {
     w.item_k0 = (int64_t *)item_k0.p;
     w.item_nk = (uint32_t *)item_nk.p;
     w.item_inc = (uint32_t *)item_inc.p;
-    w.q_unit_off = (int64_t *)q_unit_off.p;
     w.span_start = (int64_t *)span_start.p;
     w.span_len = (int64_t *)span_len.p;
     w.inc = (uint32_t *)inc.p;

@@ -37,7 +37,7 @@ DeviceContext &device_context(int dev);
 // part scratch, results), grown on demand.
 struct Workspace {
     DevBuf item_off, dim, low, up, weight, weighted, k, out_off;
-    DevBuf item_k0, item_nk, item_inc, q_unit_off;
+    DevBuf item_k0, item_nk, item_inc;
     DevBuf span_start, span_len, inc, qinfo, work, ctr, qstate, done, part_cnt, scratch;
     DevBuf out_ids, out_counts, out_scores;
     bool done_zeroed = false;

@@ -103,14 +103,14 @@ struct Tuning {
 enum : int { kListSparsePacked = 0, kListSparseWide = 1, kListDenseSmall = 2, kListDenseWide = 3,
              kListBitmap = 4, kNumLists = 5 };
 constexpr int kCtrError = 2 * kNumLists;     // ctr[2c] = items in list c, ctr[2c+1] = next
-constexpr int kCtrWords = 2 * kNumLists + 2;
+constexpr int kCtrUnits = 2 * kNumLists + 2;  // 64-bit: units handed out to queries so far
+constexpr int kCtrWords = 2 * kNumLists + 4;
 
 // Device work state of one search (all arrays sized for the batch).
 struct Work {
     int64_t *item_k0;      // [items] first key an item covers
     uint32_t *item_nk;     // [items] keys it covers (0: matches nothing)
     uint32_t *item_inc;    // [items] increment per match (1, or fixed-point weight)
-    int64_t *q_unit_off;   // [Q+1] unit count, then first unit, of every query
     int64_t *span_start;   // [units] start of the unit's sorted list (or first segment)
     int64_t *span_len;     // [units] its length (or segment count)
     uint32_t *inc;         // [units] increment per match

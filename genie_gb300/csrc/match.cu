@@ -27,12 +27,12 @@ void read_oob(unsigned long long out[4]) {
 
 // ------------------------------------------------------------------ plan
 //
-// Query compile on the device, in three launches:
+// Query compile on the device, in two launches:
 //   k_plan_items  one CTA per query: clamp every item (Query::attr /
 //                 Query::build, query/query.cc:87-113, 273-333), count the
 //                 (dim,value) lists it covers, the posting ids it touches,
 //                 and the fixed-point scale of a weighted query;
-//   k_unit_scan   one CTA: exclusive scan of the per-query list counts;
+//   (a device counter hands every query a contiguous range of units)
 //   k_plan_units  one CTA per query: one unit per covered list (a sorted
 //                 posting list, or the segment range of a compressed one),
 //                 then the bitmap/sparse/dense decision and the work lists.
@@ -124,7 +124,9 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_items(DevIndex ix, DevQue
     if (tid == 0 && GG_OK(q, W.q_cap, 12)) {
         QInfo qi;
         qi.total = (int64_t)s_total;
-        qi.unit0 = 0;
+        // the query's units: a contiguous range taken from a device counter
+        // (ranges of different queries need no order between them)
+        qi.unit0 = (int64_t)atomicAdd((unsigned long long *)&W.ctr[kCtrUnits], (unsigned long long)s_units);
         qi.n_units = (int32_t)s_units;
         qi.item0 = i0;
         qi.n_items = m;
@@ -138,38 +140,9 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_items(DevIndex ix, DevQue
         qi.parts = 1;
         qi.cls = kClsNone;
         W.qinfo[q] = qi;
-        W.q_unit_off[q] = (int64_t)s_units;
         W.done[q] = 0;
         W.qstate[q] = 0;
         if (k == 0 || k > (uint32_t)kMaxK) atomicOr(&W.ctr[kCtrError], kErrCapacity);
-    }
-}
-
-// Exclusive scan of the per-query unit counts (one CTA, any number of queries).
-__global__ void __launch_bounds__(1024) k_unit_scan(DevQueries Q, Work W) {
-    __shared__ uint32_t s_tmp[48];
-    __shared__ int64_t s_carry;
-    const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
-    if (threadIdx.x == 0) s_carry = 0;
-    __syncthreads();
-    for (int64_t b = 0; b < nq; b += blockDim.x) {
-        const int64_t q = b + threadIdx.x;
-        const int64_t v = q < nq ? W.q_unit_off[q] : 0;
-        // units per query fit 32 bits; the running offset is 64-bit
-        uint32_t tot = 0;
-        const uint32_t ex = block_excl_scan((uint32_t)v, s_tmp, &tot);
-        const int64_t off = s_carry + ex;
-        if (q < nq) {
-            W.q_unit_off[q] = off;
-            W.qinfo[q].unit0 = off;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) s_carry += tot;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        W.q_unit_off[nq] = s_carry;
-        if (s_carry > W.units_cap) atomicOr(&W.ctr[kCtrError], kErrUnits);
     }
 }
 
@@ -180,7 +153,9 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_units(DevIndex ix, DevQue
     if (q >= nq) return;
     const uint32_t tid = threadIdx.x, nt = blockDim.x;
     QInfo qi = W.qinfo[q];
-    const bool fits = W.q_unit_off[nq] <= W.units_cap;
+    const int64_t units = (int64_t)*(volatile unsigned long long *)&W.ctr[kCtrUnits];
+    const bool fits = units <= W.units_cap;
+    if (q == 0 && tid == 0 && !fits) atomicOr(&W.ctr[kCtrError], kErrUnits);
     if (fits) {
         int64_t base = qi.unit0;
         const int64_t i1 = qi.item0 + qi.n_items;
@@ -992,49 +967,77 @@ bool bitmap_fits(const Tuning &t, int64_t n_objects) {
     return bm_layout(n_objects, (uint32_t)t.bitmap_multi_slots).bytes <= limit;
 }
 
-int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &tun,
-                 int num_sms, cudaStream_t s, cudaEvent_t *ev) {
-    if (Q.n_queries <= 0) return 0;
+// Per-launch tuning: SM count, and whether the bitmap kernel fits this index.
+Tuning launch_tuning(const DevIndex &ix, const Tuning &tun, int num_sms) {
     Tuning t = tun;
     t.num_sms = num_sms;
     t.bitmap_ready = bitmap_fits(t, ix.n_objects) ? 1 : 0;
     if (!t.bitmap_ready) t.bitmap_bits = 0;
-    int launches = 0;
-    if (ev) cudaEventRecord(ev[0], s);
+    return t;
+}
+
+int launch_plan(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t, cudaStream_t s) {
     cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), s);
     k_plan_items<<<Q.n_queries, kPlanThreads, 0, s>>>(ix, Q, W, t);
-    k_unit_scan<<<1, 1024, 0, s>>>(Q, W);
     k_plan_units<<<Q.n_queries, kPlanThreads, 0, s>>>(ix, Q, W, t);
-    launches += 3;
-    if (ev) cudaEventRecord(ev[1], s);
+    return 2;
+}
+
+// One match kernel (kListBitmap .. kListDenseWide) as a persistent grid.
+int launch_list(int list, const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t, int num_sms,
+                cudaStream_t s) {
     // persistent grids: as many CTAs as fit on every SM at once
     auto grid = [&](const void *fn, int threads, size_t smem) {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
         return num_sms * std::max(1, per_sm);
     };
-    const size_t sp = sparse_smem_bytes(t, true), sw = sparse_smem_bytes(t, false);
-    const size_t dp = dense_smem_bytes(t, true), dw = dense_smem_bytes(t, false);
-    if (t.bitmap_bits > 0) {
+    const bool wide_ctas = t.sparse_threads == 1024;
+    switch (list) {
+    case kListBitmap: {
+        if (t.bitmap_bits <= 0) return 0;
         const size_t bp = bm_layout(ix.n_objects, (uint32_t)t.bitmap_multi_slots).bytes;
         k_bitmap<<<num_sms, kBmThreads, bp, s>>>(ix, Q, W, t);
+        return 1;
     }
-    if (ev) cudaEventRecord(ev[2], s);
-    if (t.sparse_threads == 1024) {
-        k_sparse<true, 1024><<<grid((const void *)k_sparse<true, 1024>, 1024, sp), 1024, sp, s>>>(ix, Q, W, t);
-        if (ev) cudaEventRecord(ev[3], s);
-        k_sparse<false, 1024><<<grid((const void *)k_sparse<false, 1024>, 1024, sw), 1024, sw, s>>>(ix, Q, W, t);
-    } else {
-        k_sparse<true, 512><<<grid((const void *)k_sparse<true, 512>, 512, sp), 512, sp, s>>>(ix, Q, W, t);
-        if (ev) cudaEventRecord(ev[3], s);
-        k_sparse<false, 512><<<grid((const void *)k_sparse<false, 512>, 512, sw), 512, sw, s>>>(ix, Q, W, t);
+    case kListSparsePacked: {
+        const size_t sp = sparse_smem_bytes(t, true);
+        if (wide_ctas) k_sparse<true, 1024><<<grid((const void *)k_sparse<true, 1024>, 1024, sp), 1024, sp, s>>>(ix, Q, W, t);
+        else k_sparse<true, 512><<<grid((const void *)k_sparse<true, 512>, 512, sp), 512, sp, s>>>(ix, Q, W, t);
+        return 1;
     }
-    if (ev) cudaEventRecord(ev[4], s);
-    k_dense<true><<<grid((const void *)k_dense<true>, t.dense_threads, dp), t.dense_threads, dp, s>>>(ix, Q, W, t);
-    if (ev) cudaEventRecord(ev[5], s);
-    k_dense<false><<<grid((const void *)k_dense<false>, t.dense_threads, dw), t.dense_threads, dw, s>>>(ix, Q, W, t);
-    if (ev) cudaEventRecord(ev[6], s);
-    launches += t.bitmap_bits > 0 ? 5 : 4;
+    case kListSparseWide: {
+        const size_t sw = sparse_smem_bytes(t, false);
+        if (wide_ctas) k_sparse<false, 1024><<<grid((const void *)k_sparse<false, 1024>, 1024, sw), 1024, sw, s>>>(ix, Q, W, t);
+        else k_sparse<false, 512><<<grid((const void *)k_sparse<false, 512>, 512, sw), 512, sw, s>>>(ix, Q, W, t);
+        return 1;
+    }
+    case kListDenseSmall: {
+        const size_t dp = dense_smem_bytes(t, true);
+        k_dense<true><<<grid((const void *)k_dense<true>, t.dense_threads, dp), t.dense_threads, dp, s>>>(ix, Q, W, t);
+        return 1;
+    }
+    default: {
+        const size_t dw = dense_smem_bytes(t, false);
+        k_dense<false><<<grid((const void *)k_dense<false>, t.dense_threads, dw), t.dense_threads, dw, s>>>(ix, Q, W, t);
+        return 1;
+    }
+    }
+}
+
+int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &tun,
+                 int num_sms, cudaStream_t s, cudaEvent_t *ev) {
+    if (Q.n_queries <= 0) return 0;
+    const Tuning t = launch_tuning(ix, tun, num_sms);
+    int launches = 0;
+    if (ev) cudaEventRecord(ev[0], s);
+    launches += launch_plan(ix, Q, W, t, s);
+    if (ev) cudaEventRecord(ev[1], s);
+    const int order[kNumLists] = {kListBitmap, kListSparsePacked, kListSparseWide, kListDenseSmall, kListDenseWide};
+    for (int i = 0; i < kNumLists; ++i) {
+        launches += launch_list(order[i], ix, Q, W, t, num_sms, s);
+        if (ev) cudaEventRecord(ev[2 + i], s);
+    }
     return launches;
 }
 

@@ -32,7 +32,7 @@ constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
 // Byte layout of the workspace inside the array.
 struct NaLayout {
-    size_t item_k0, item_nk, item_inc, q_unit_off, span_start, span_len, inc, qinfo, work, ctr, qstate, done,
+    size_t item_k0, item_nk, item_inc, span_start, span_len, inc, qinfo, work, ctr, qstate, done,
         part_cnt, scratch, total;
 };
 
@@ -42,7 +42,6 @@ constexpr NaLayout na_layout() {
     L.item_k0 = o;    o += align256(kNaMaxItems * 8);
     L.item_nk = o;    o += align256(kNaMaxItems * 4);
     L.item_inc = o;   o += align256(kNaMaxItems * 4);
-    L.q_unit_off = o; o += align256((kNaMaxQueries + 1) * 8);
     L.span_start = o; o += align256(kNaMaxUnits * 8);
     L.span_len = o;   o += align256(kNaMaxUnits * 8);
     L.inc = o;        o += align256(kNaMaxUnits * 4);
@@ -109,7 +108,6 @@ extern "C" int genie_search_noalloc(genie_index *ix, const genie_queries *q, con
     w.item_k0 = (int64_t *)(base + kNa.item_k0);
     w.item_nk = (uint32_t *)(base + kNa.item_nk);
     w.item_inc = (uint32_t *)(base + kNa.item_inc);
-    w.q_unit_off = (int64_t *)(base + kNa.q_unit_off);
     w.span_start = (int64_t *)(base + kNa.span_start);
     w.span_len = (int64_t *)(base + kNa.span_len);
     w.inc = (uint32_t *)(base + kNa.inc);
