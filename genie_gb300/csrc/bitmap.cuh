@@ -134,8 +134,9 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
     const BmLayout L = bm_layout(ix.n_objects, mslots);
     uint32_t *bm = (uint32_t *)(smem + L.bm);
     uint32_t *mt = (uint32_t *)(smem + L.mt);
-    // chunk entry: posting position of its first id << 6 | ids in it (1..32)
-    uint64_t *chunk = (uint64_t *)(smem + L.chunk);
+    // chunk entry: posting position of its first id, ids in it (1..32); an
+    // empty entry (0, 0) reads ids [0, 32) and counts none of them
+    uint2 *chunk = (uint2 *)(smem + L.chunk);
     uint32_t *mlist = (uint32_t *)(smem + L.mlist);
     uint64_t *cand = (uint64_t *)(smem + L.chunk);                  // [0, kCandCap)
     uint32_t *tie_ids = (uint32_t *)(cand + kCandCap);               // [0, kCandCap)
@@ -143,7 +144,6 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
     SelectScratch &ss = *(SelectScratch *)(smem + L.ss);
     uint32_t *hist = ss.hist;
     __shared__ uint32_t s_multi, s_ovf, s_n, s_big;
-    __shared__ uint32_t s_spare[32];
     __shared__ BmQuery s_qd[2];
 
     const uint32_t tid = threadIdx.x, lane = lane_id(), warp = warp_id();
@@ -200,12 +200,12 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
         const uint32_t c0 = block_excl_scan(nch, ss.tmp, &n_chunks);     // ends with a barrier
         const BmQuery d = s_qd[it & 1];
         for (uint32_t c = 0; c < nch && c0 + c < kBmChunks; ++c)
-            chunk[c0 + c] = ((uint64_t)(sp_start + 32 * (int64_t)c) << 6) |
-                            (uint64_t)min((int64_t)32, sp_len - 32 * (int64_t)c);
+            chunk[c0 + c] = make_uint2((uint32_t)(sp_start + 32 * (int64_t)c),
+                                       (uint32_t)min((int64_t)32, sp_len - 32 * (int64_t)c));
         // empty entries up to whole rounds of every warp, so rounds need no bounds
         const uint32_t round_ids = 32u * kBmRound;
         const uint32_t padded = min(kBmChunks, (n_chunks + round_ids - 1) / round_ids * round_ids);
-        for (uint32_t c = n_chunks + tid; c < padded; c += kBmThreads) chunk[c] = 0ull;
+        for (uint32_t c = n_chunks + tid; c < padded; c += kBmThreads) chunk[c] = make_uint2(0u, 0u);
         // spans of the next query, in flight during this one
         sp_start = 0;
         sp_len = 0;
@@ -247,23 +247,28 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
             s_ovf = 1;
             return 0u;
         };
+        // Integer work per id is what bounds this loop, so it is kept small:
+        // every lane loads 32 ids past its entry's position (the id array is
+        // padded for that, and every value there is a valid id), and a lane
+        // past the entry's count ORs an empty mask into the word of whatever
+        // id it read.  Ids are below n_objects (checked when an index is
+        // built or loaded), so every word index is inside the bitmap.
         const uint32_t nc = min(n_chunks, kBmChunks);
+        const uint32_t *lane_ids = ix.ids + lane;
         for (uint32_t j0 = warp; j0 < nc; j0 += 32 * kBmRound) {
             uint32_t v[kBmRound], ok = 0;
 #pragma unroll
             for (int r = 0; r < kBmRound; ++r) {
-                const uint64_t e = chunk[j0 + r * 32];
-                const bool g = lane < (uint32_t)(e & 63u);
-                v[r] = __ldg(ix.ids + (g ? (int64_t)(e >> 6) + lane : 0));
-                ok |= (g ? 1u : 0u) << r;
+                const uint2 e = chunk[j0 + r * 32];
+                v[r] = __ldg(lane_ids + e.x);
+                ok |= lane < e.y ? 1u << r : 0u;
             }
             uint32_t old[kBmRound];
 #pragma unroll
             for (int r = 0; r < kBmRound; ++r) {      // independent atomics, all in flight
-                bool g = (ok >> r & 1u) != 0;
-                g = g && GG_OK(v[r] >> 5, words, 15);
-                const uint32_t m = g ? 1u << (v[r] & 31) : 0u;
-                old[r] = atomicOr(g ? &bm[v[r] >> 5] : &s_spare[lane], m) & m;
+                if (!GG_OK(v[r] >> 5, words, 15)) v[r] = 0;
+                const uint32_t m = __funnelshift_l(0u, (ok >> r) & 1u, v[r]);     // (ok bit r) << (id % 32)
+                old[r] = atomicOr(&bm[v[r] >> 5], m) & m;
             }
             uint32_t rep = 0;
 #pragma unroll

@@ -253,14 +253,14 @@ int build_device_index(const int32_t *values, int64_t n, int32_t d, genie_index 
     uint32_t *d_H = nullptr;
     int64_t *d_tot = nullptr, *d_keyoff = nullptr;
     if ((e = cudaMalloc(&d_H, (size_t)chunks * kMaxBins * 4)) || (e = cudaMalloc(&d_tot, kMaxBins * 8)) ||
-        (e = ix->d_ids.reserve(cells * 4 + 64)) || (e = ix->d_key_off.reserve((size_t)(nk + 1) * 8))) {
+        (e = ix->d_ids.reserve(cells * 4 + kIdsPadBytes)) || (e = ix->d_key_off.reserve((size_t)(nk + 1) * 8))) {
         cudaFree(d_H);
         cudaFree(d_tot);
         cleanup();
         return e == cudaErrorMemoryAllocation ? fail(GENIE_ERR_GPU_ALLOC, "device index build: out of memory")
                                               : cuda_fail(e, "device index build");
     }
-    cudaMemset(ix->d_ids.p, 0, cells * 4 + 64);
+    cudaMemset(ix->d_ids.p, 0, cells * 4 + kIdsPadBytes);
     d_keyoff = (int64_t *)ix->d_key_off.p;
     uint32_t *d_ids = (uint32_t *)ix->d_ids.p;
     for (int32_t j = 0; j < d; ++j) {

@@ -201,7 +201,9 @@ int upload_index(genie_index *ix, int64_t device_ids) {
     const HostIndex &h = ix->host;
     cudaError_t e;
     if (device_ids < 0) {       // ids and key offsets come from the host mirror
-        const size_t ids_bytes = h.ids.size() * 4 + 64;     // padded for vector loads
+        // padded: a warp reads 32 ids from any list position, and the padding
+        // (zeros) holds valid ids
+        const size_t ids_bytes = h.ids.size() * 4 + kIdsPadBytes;
         if ((e = ix->d_ids.reserve(ids_bytes))) return cuda_fail(e, "index ids");
         if ((e = cudaMemset(ix->d_ids.p, 0, ids_bytes))) return cuda_fail(e, "index ids");
         if (!h.ids.empty() && (e = cudaMemcpy(ix->d_ids.p, h.ids.data(), h.ids.size() * 4, cudaMemcpyHostToDevice)))

@@ -192,7 +192,8 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_units(DevIndex ix, DevQue
             const int64_t ps = (total + cap - 1) / cap;
             if (total <= T.sparse_max_total && total * 4 <= ix.n_objects * 3 && packed && !ix.codec &&
                 T.bitmap_bits > 0 && T.bitmap_ready && ix.n_objects <= T.bitmap_bits &&
-                qi.n_units <= (int32_t)kBmSpanCap && total <= (int64_t)kBmMaxIds) {
+                qi.n_units <= (int32_t)kBmSpanCap && total <= (int64_t)kBmMaxIds &&
+                ix.n_ids <= (int64_t)0xFFFFFFFFll - 64) {       // posting positions in 32 bits
                 // presence bitmap over the whole id space + a table of repeated ids
                 qi.cls = kClsSparse;
                 qi.parts = 1;

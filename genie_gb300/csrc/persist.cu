@@ -135,6 +135,25 @@ int load_index(const char *path, genie_index *ix) {
     if (!ok) return fail(GENIE_ERR_IO, "%s is truncated", path);
     if (sum != want) return fail(GENIE_ERR_IO, "%s fails its checksum", path);
     if (h.key_base.back() != n_keys || h.key_off.back() < 0) return fail(GENIE_ERR_IO, "%s is inconsistent", path);
+    // the kernels index shared memory by object id and search lists by
+    // bisection: a file whose checksum holds must still describe a valid index
+    for (int32_t d = 0; d < h.n_dims; ++d) {
+        const int64_t width = (int64_t)h.dim_max[d] - h.dim_min[d] + 1;
+        if (h.key_base[d] < 0 || h.key_base[d + 1] < h.key_base[d] ||
+            (width > 0 && h.key_base[d] + width > h.key_base[d + 1]))
+            return fail(GENIE_ERR_IO, "%s is inconsistent (dimension %d)", path, d);
+    }
+    if (!ix->codec) {
+        if (h.key_off[0] != 0 || h.key_off.back() != ix->n_ids)
+            return fail(GENIE_ERR_IO, "%s is inconsistent (list offsets)", path);
+        for (int64_t k = 0; k < n_keys; ++k) {
+            const int64_t a = h.key_off[k], b = h.key_off[k + 1];
+            if (b < a) return fail(GENIE_ERR_IO, "%s is inconsistent (list %lld)", path, (long long)k);
+            for (int64_t p = a; p < b; ++p)
+                if ((int64_t)h.ids[p] >= h.n_objects || (p > a && h.ids[p] < h.ids[p - 1]))
+                    return fail(GENIE_ERR_IO, "%s is inconsistent (list %lld)", path, (long long)k);
+        }
+    }
     ix->is_bag = (flags & 1u) != 0;
     if (!ix->codec) return upload_index(ix);
     return upload_compressed(ix, words, key_seg, seg_word_off, seg_first, seg_len);
