@@ -37,6 +37,8 @@ constexpr uint32_t kBmThreads = 1024;
 constexpr uint32_t kBmChunks = 4096;      // 32-id chunks per query on this path
 constexpr uint32_t kBmProbe = 128;        // longest probe run of the repeated-id table
 constexpr int kBmRound = 16;              // chunk loads in flight per lane
+constexpr uint32_t kBmDescRing = 128;     // query descriptors kept in shared memory
+constexpr uint32_t kBmDescFill = 64;      // descriptors loaded at a time
 
 // Byte offsets of the shared-memory regions (host and device agree).
 struct BmLayout {
@@ -144,7 +146,7 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
     SelectScratch &ss = *(SelectScratch *)(smem + L.ss);
     uint32_t *hist = ss.hist;
     __shared__ uint32_t s_multi, s_ovf, s_n, s_big;
-    __shared__ BmQuery s_qd[2];
+    __shared__ BmQuery s_desc[kBmDescRing];     // item i of this CTA in slot i % kBmDescRing
 
     const uint32_t tid = threadIdx.x, lane = lane_id(), warp = warp_id();
     const uint32_t G = gridDim.x, n_work = W.ctr[2 * kListBitmap];
@@ -153,52 +155,55 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
     const uint32_t mcap = mslots / 2;
     const uint32_t words = L.bm_words;
 
-    auto load_q = [&](uint32_t q) {      // thread 0
-        BmQuery d{};
-        d.q = q;
-        if (GG_OK(q, W.q_cap, 16)) {
-            const QInfo qi = W.qinfo[q];
-            d.k = qi.k;
-            d.n_units = (uint32_t)qi.n_units;
-            d.unit0 = qi.unit0;
-            d.out_off = Q.out_off[q];
+    // descriptors of this CTA's items [i0, i0 + kBmDescFill) into their slots
+    // (block-uniform call; a later barrier publishes them).  Loaded in bulk so
+    // that no load of a later query waits in a register through a query.
+    auto fill_desc = [&](uint32_t i0) {
+        if (tid < kBmDescFill) {
+            const uint32_t i = i0 + tid;
+            BmQuery d{};
+            d.q = 0xFFFFFFFFu;
+            const uint64_t w = (uint64_t)blockIdx.x + (uint64_t)i * G;
+            if (w < n_work && GG_OK(w, W.work_stride, 16)) {
+                const uint32_t q = work[w].x;
+                if (GG_OK(q, W.q_cap, 16)) {
+                    const QInfo qi = W.qinfo[q];
+                    d.q = q;
+                    d.k = qi.k;
+                    d.n_units = (uint32_t)qi.n_units;
+                    d.unit0 = qi.unit0;
+                    d.out_off = Q.out_off[q];
+                }
+            }
+            s_desc[i % kBmDescRing] = d;
         }
-        return d;
-    };
-    auto work_q = [&](uint32_t i) -> uint32_t {    // query of this CTA's i-th item, or ~0
-        const uint32_t w = blockIdx.x + i * G;
-        return (w < n_work && GG_OK(w, W.work_stride, 16)) ? work[w].x : 0xFFFFFFFFu;
     };
 
     for (uint32_t i = tid; i < words / 4; i += kBmThreads) ((uint4 *)bm)[i] = make_uint4(0u, 0u, 0u, 0u);
     for (uint32_t i = tid; i < mslots; i += kBmThreads) mt[i] = 0u;
     for (uint32_t i = tid; i < 256; i += kBmThreads) hist[i] = 0u;
-    uint32_t q_next2 = 0xFFFFFFFFu;      // thread 0: query two items ahead
-    BmQuery qd_next{};                   // thread 0: descriptor one item ahead
     if (tid == 0) {
         s_multi = 0;
         s_ovf = 0;
-        s_qd[0] = load_q(work_q(0));
-        const uint32_t q1 = work_q(1);
-        if (q1 != 0xFFFFFFFFu) qd_next = load_q(q1);
-        q_next2 = work_q(2);
     }
+    fill_desc(0);
     __syncthreads();
     // spans of this thread's list in the current query (prefetched one query ahead)
     int64_t sp_start = 0, sp_len = 0;
-    if (tid < s_qd[0].n_units && GG_OK(s_qd[0].unit0 + tid, W.units_cap, 9)) {
-        sp_start = W.span_start[s_qd[0].unit0 + tid];
-        sp_len = W.span_len[s_qd[0].unit0 + tid];
+    if (tid < s_desc[0].n_units && GG_OK(s_desc[0].unit0 + tid, W.units_cap, 9)) {
+        sp_start = W.span_start[s_desc[0].unit0 + tid];
+        sp_len = W.span_len[s_desc[0].unit0 + tid];
     }
 
     for (uint32_t it = 0; blockIdx.x + it * G < n_work; ++it) {
         const bool more = blockIdx.x + (it + 1) * G < n_work;
-        if (tid == 0 && more) s_qd[(it + 1) & 1] = qd_next;
+        // the next descriptors, before the span loads of item it + 1 read them;
+        // the slots they take held items finished long ago
+        if (more && (it + 1) % kBmDescFill == 0) fill_desc(it + 1);
         // ---- stage: chunk entries of every list
         const uint32_t nch = (uint32_t)((sp_len + 31) / 32);
         uint32_t n_chunks = 0;
         const uint32_t c0 = block_excl_scan(nch, ss.tmp, &n_chunks);     // ends with a barrier
-        const BmQuery d = s_qd[it & 1];
         for (uint32_t c = 0; c < nch && c0 + c < kBmChunks; ++c)
             chunk[c0 + c] = make_uint2((uint32_t)(sp_start + 32 * (int64_t)c),
                                        (uint32_t)min((int64_t)32, sp_len - 32 * (int64_t)c));
@@ -210,14 +215,12 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
         sp_start = 0;
         sp_len = 0;
         if (more) {
-            const BmQuery dn = s_qd[(it + 1) & 1];
+            const BmQuery dn = s_desc[(it + 1) % kBmDescRing];
             if (tid < dn.n_units && GG_OK(dn.unit0 + tid, W.units_cap, 9)) {
                 sp_start = W.span_start[dn.unit0 + tid];
                 sp_len = W.span_len[dn.unit0 + tid];
             }
         }
-        uint32_t q_next3 = 0xFFFFFFFFu;
-        if (tid == 0) q_next3 = work_q(it + 3);
         __syncthreads();
 
         // ---- stream
@@ -284,16 +287,25 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
                 }
             }
         }
-        if (tid == 0 && q_next2 != 0xFFFFFFFFu) qd_next = load_q(q_next2);     // lands during selection
         __syncthreads();
 
         // ---- exact top-k of this query
+        const BmQuery d = s_desc[it % kBmDescRing];
         const uint32_t k = d.k, q = d.q;
         const int64_t out_off = d.out_off;
         const uint32_t n_multi = min(s_multi, mcap);
-        bool failed = s_ovf != 0 || n_chunks > kBmChunks;
+        const bool ovf = s_ovf != 0;
+        bool failed = ovf || n_chunks > kBmChunks;
         uint32_t nres = 0, n_hi = 0, cstar = 0;     // keys cand[0, n_hi), then tie ids at c*
         if (!failed && n_multi >= k) {
+            // tie ids go to id-range buckets (counting sort): bucket b holds ids
+            // [b << sh, (b+1) << sh); the counters borrow the first bitmap
+            // words, cleared while warp 0 finds c*
+            const uint32_t nb = min(1024u, words);
+            uint32_t sh = 0;
+            while (((uint32_t)(ix.n_objects - 1) >> sh) >= nb) ++sh;
+            uint32_t *bcnt = bm;
+            for (uint32_t x = tid; x < nb; x += kBmThreads) bcnt[x] = 0u;
             if (warp == 0) find_digit(ss, k, true);     // k-th largest count
             if (tid == 0) {
                 s_n = 0;
@@ -302,14 +314,6 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
             __syncthreads();
             cstar = ss.sc[0];
             const uint32_t above = ss.sc[1], n_eq = ss.sc[2];
-            // tie ids go to id-range buckets (counting sort): bucket b holds ids
-            // [b << sh, (b+1) << sh); the counters borrow the first bitmap words
-            const uint32_t nb = min(1024u, words);
-            uint32_t sh = 0;
-            while (((uint32_t)(ix.n_objects - 1) >> sh) >= nb) ++sh;
-            uint32_t *bcnt = bm;
-            for (uint32_t x = tid; x < nb; x += kBmThreads) bcnt[x] = 0u;
-            __syncthreads();
             // entries above c* to cand (warp-aggregated); count the ties per bucket
             for (uint32_t b = 0; b < n_multi; b += kBmThreads) {
                 const uint32_t x = b + tid;
@@ -330,7 +334,7 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
                 const uint32_t e = x < n_multi ? mt[mlist[x]] : 0u;
                 if (e != 0u && (e & 255u) == cstar) {
                     const uint32_t at = atomicAdd(&bcnt[(e >> 8) >> sh], 1u);
-                    if (GG_OK(at, kCandCap, 19)) tie_ids[at] = e >> 8;
+                    if (at < (uint32_t)kCandCap) tie_ids[at] = e >> 8;
                 }
             }
             if (warp == 0 && above <= 64) warp_sort_desc64(cand, above);
@@ -408,17 +412,15 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
         // ---- clear the state for the next query
         __syncthreads();
         for (uint32_t x = tid; x < words / 4; x += kBmThreads) ((uint4 *)bm)[x] = make_uint4(0u, 0u, 0u, 0u);
-        if (s_ovf) {
+        if (ovf) {
             for (uint32_t x = tid; x < mslots; x += kBmThreads) mt[x] = 0u;
         } else {
-            for (uint32_t x = tid; x < min(s_multi, mcap); x += kBmThreads) mt[mlist[x]] = 0u;
+            for (uint32_t x = tid; x < n_multi; x += kBmThreads) mt[mlist[x]] = 0u;
         }
         for (uint32_t x = tid; x < 256; x += kBmThreads) hist[x] = 0u;
-        __syncthreads();     // s_multi read above before it is reset
-        if (tid == 0) {
+        if (tid == 0) {      // every thread read both right after the stream, barriers ago
             s_multi = 0;
             s_ovf = 0;
-            q_next2 = q_next3;
         }
         __syncthreads();
     }

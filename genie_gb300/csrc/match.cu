@@ -964,7 +964,10 @@ bool bitmap_fits(const Tuning &t, int64_t n_objects) {
         if (cudaFuncGetAttributes(&a, (const void *)k_bitmap) == cudaSuccess) st = a.sharedSizeBytes;
         limit = (size_t)optin - st;
     }
-    if (t.bitmap_bits <= 0 || n_objects > t.bitmap_bits || t.bitmap_multi_slots <= 0) return false;
+    // the table's entries (half its slots) fit the tie and candidate buffers
+    if (t.bitmap_bits <= 0 || n_objects > t.bitmap_bits || t.bitmap_multi_slots <= 0 ||
+        t.bitmap_multi_slots > 2 * kCandCap)
+        return false;
     return bm_layout(n_objects, (uint32_t)t.bitmap_multi_slots).bytes <= limit;
 }
 
