@@ -220,6 +220,26 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *s_tmp,
     return r;
 }
 
+// Exclusive scan over a group of whole warps (G::rank() order); tmp holds 33
+// words.  Starts with a barrier, so back-to-back calls may share tmp.
+template <class G>
+__device__ uint32_t group_excl_scan(uint32_t v, uint32_t *tmp, uint32_t *total) {
+    const uint32_t r = G::rank(), w = r >> 5, nw = G::size() >> 5, l = lane_id();
+    const uint32_t incl = warp_incl_scan(v);
+    G::sync();
+    if (l == 31) tmp[w] = incl;
+    G::sync();
+    if (w == 0) {
+        const uint32_t x = l < nw ? tmp[l] : 0u;
+        const uint32_t xi = warp_incl_scan(x);
+        if (l < nw) tmp[l] = xi - x;
+        if (l == 31) tmp[32] = xi;
+    }
+    G::sync();
+    if (total) *total = tmp[32];
+    return tmp[w] + incl - v;
+}
+
 // Warp-aggregated shared-memory histogram increment: lanes holding the same
 // bin combine into one atomic (__match_any_sync).  All 32 lanes must call.
 __device__ __forceinline__ void hist_add(uint32_t *hist, uint32_t bin, bool active) {

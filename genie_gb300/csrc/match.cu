@@ -27,19 +27,17 @@ void read_oob(unsigned long long out[4]) {
 
 // ------------------------------------------------------------------ plan
 //
-// Query compile on the device, in two launches:
-//   k_plan_items  one CTA per query: clamp every item (Query::attr /
-//                 Query::build, query/query.cc:87-113, 273-333), count the
-//                 (dim,value) lists it covers, the posting ids it touches,
-//                 and the fixed-point scale of a weighted query;
-//   (a device counter hands every query a contiguous range of units)
-//   k_plan_units  one CTA per query: one unit per covered list (a sorted
-//                 posting list, or the segment range of a compressed one),
-//                 then the bitmap/sparse/dense decision and the work lists.
+// Query compile on the device, one CTA per query in one launch: clamp every
+// item (Query::attr / Query::build, query/query.cc:87-113, 273-333), count the
+// (dim,value) lists it covers and the posting ids it touches, the fixed-point
+// scale of a weighted query; take a contiguous range of units from a device
+// counter (ranges of different queries need no order between them); write one
+// unit per covered list (a sorted posting list, or the segment range of a
+// compressed one); then the bitmap/sparse/dense decision and the work lists.
 // A range item covers several lists whose concatenation is not sorted, so
 // every later search inside a span happens per unit.
 
-constexpr int kPlanThreads = 128;
+constexpr int kPlanThreads = 256;
 
 // Id-range parts of a dense query: one per dense_part_work posting ids, more
 // when the batch has too few queries to give every SM a part, at most one per
@@ -55,13 +53,14 @@ __device__ __forceinline__ int64_t dense_parts(int64_t total, int64_t ntiles, in
     return pd < 1 ? 1 : pd;
 }
 
-__global__ void __launch_bounds__(kPlanThreads) k_plan_items(DevIndex ix, DevQueries Q, Work W, Tuning T) {
-    __shared__ unsigned long long s_total, s_units;
+__global__ void __launch_bounds__(kPlanThreads, 4) k_plan(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+    __shared__ unsigned long long s_total, s_units, s_unit0;
     __shared__ unsigned int s_maxw, s_bad;
+    __shared__ uint32_t s_tmp[48];
     const int64_t q = blockIdx.x;
     const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
     if (q >= nq) return;
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
+    const uint32_t tid = threadIdx.x, nt = blockDim.x, lane = lane_id();
     const int64_t i0 = Q.item_off[q], i1 = Q.item_off[q + 1];
     const int32_t m = (int32_t)(i1 - i0);
     const uint32_t k = Q.k ? Q.k[q] : (Q.dyn ? Q.dyn[1] : Q.uniform_k);
@@ -92,11 +91,15 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_items(DevIndex ix, DevQue
         scale = 31 - e;
         if (s_bad && tid == 0) atomicOr(&W.ctr[kCtrError], kErrWeight);
     }
+    // items: key range, touched ids; this thread's first item stays in
+    // registers, later ones (queries of more than nt items) go through W
     uint64_t total = 0, units = 0;
+    int64_t k0_first = 0, a_first = 0, e_first = 0;     // a, e: list offsets around the keys
+    uint32_t nk_first = 0, inc_first = 1;
     for (int64_t i = i0 + tid; i < i1; i += nt) {
         if (!GG_OK(i, W.items_cap, 7)) break;
         int32_t d = Q.dim[i], lo = Q.low[i], hi = Q.up[i];
-        int64_t k0 = 0, nk = 0;
+        int64_t k0 = 0, nk = 0, a = 0, e = 0;
         if (d >= 0 && d < ix.n_dims) {
             int32_t mn = ix.dim_min[d], mx = ix.dim_max[d];
             if (!(lo > hi || lo > mx || hi < mn)) {
@@ -104,84 +107,98 @@ __global__ void __launch_bounds__(kPlanThreads) k_plan_items(DevIndex ix, DevQue
                 if (hi > mx) hi = mx;
                 k0 = ix.key_base[d] + ((int64_t)lo - mn);
                 nk = (int64_t)hi - lo + 1;
-                total += (uint64_t)(ix.key_off[k0 + nk] - ix.key_off[k0]);
+                a = ix.key_off[k0];
+                e = ix.key_off[k0 + nk];
+                total += (uint64_t)(e - a);
             }
         }
-        W.item_k0[i] = k0;
-        W.item_nk[i] = (uint32_t)nk;
         uint32_t inc = 1;
         if (weighted) inc = (uint32_t)__double2ll_rn(ldexp((double)Q.weight[i], scale));
-        W.item_inc[i] = inc;
+        if (i == i0 + tid) {
+            k0_first = k0;
+            nk_first = (uint32_t)nk;
+            inc_first = inc;
+            a_first = a;
+            e_first = e;
+        } else {
+            W.item_k0[i] = k0;
+            W.item_nk[i] = (uint32_t)nk;
+            W.item_inc[i] = inc;
+        }
         units += (uint64_t)nk;
     }
     total = warp_sum_u64(total);
     units = warp_sum_u64(units);
-    if (lane_id() == 0) {
+    if (lane == 0) {
         atomicAdd(&s_total, (unsigned long long)total);
         atomicAdd(&s_units, (unsigned long long)units);
     }
     __syncthreads();
-    if (tid == 0 && GG_OK(q, W.q_cap, 12)) {
-        QInfo qi;
-        qi.total = (int64_t)s_total;
-        // the query's units: a contiguous range taken from a device counter
-        // (ranges of different queries need no order between them)
-        qi.unit0 = (int64_t)atomicAdd((unsigned long long *)&W.ctr[kCtrUnits], (unsigned long long)s_units);
-        qi.n_units = (int32_t)s_units;
-        qi.item0 = i0;
-        qi.n_items = m;
-        qi.k = k;
-        qi.scale = scale;
-        qi.flags = weighted ? kFlagWeighted : 0;
-        // bound on any object's count: one match per item on a one-value-per-dim
-        // table; on a bag table, every covered list may repeat the object
-        const int64_t bound = ix.is_bag ? (int64_t)s_units * ix.mult_max : (int64_t)m;
-        if (!weighted && bound <= 255) qi.flags |= kFlagSmallCount;
-        qi.parts = 1;
-        qi.cls = kClsNone;
-        W.qinfo[q] = qi;
-        W.done[q] = 0;
-        W.qstate[q] = 0;
-        if (k == 0 || k > (uint32_t)kMaxK) atomicOr(&W.ctr[kCtrError], kErrCapacity);
-    }
-}
-
-__global__ void __launch_bounds__(kPlanThreads) k_plan_units(DevIndex ix, DevQueries Q, Work W, Tuning T) {
-    __shared__ uint32_t s_tmp[48];
-    const int64_t q = blockIdx.x;
-    const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
-    if (q >= nq) return;
-    const uint32_t tid = threadIdx.x, nt = blockDim.x;
-    QInfo qi = W.qinfo[q];
-    const int64_t units = (int64_t)*(volatile unsigned long long *)&W.ctr[kCtrUnits];
-    const bool fits = units <= W.units_cap;
-    if (q == 0 && tid == 0 && !fits) atomicOr(&W.ctr[kCtrError], kErrUnits);
+    if (tid == 0) s_unit0 = atomicAdd((unsigned long long *)&W.ctr[kCtrUnits], s_units);
+    __syncthreads();
+    const int64_t unit0 = (int64_t)s_unit0, n_units = (int64_t)s_units;
+    total = s_total;
+    const bool fits = unit0 + n_units <= W.units_cap;
+    if (tid == 0 && !fits) atomicOr(&W.ctr[kCtrError], kErrUnits);
+    // one unit per covered list
     if (fits) {
-        int64_t base = qi.unit0;
-        const int64_t i1 = qi.item0 + qi.n_items;
-        for (int64_t c = qi.item0; c < i1; c += nt) {
+        int64_t base = unit0;
+        for (int64_t c = i0; c < i1; c += nt) {
             const int64_t i = c + tid;
-            const uint32_t nk = i < i1 ? W.item_nk[i] : 0u;
+            uint32_t nk = 0, inc = 1;
+            int64_t k0 = 0;
+            if (i < i1) {
+                if (c == i0) {
+                    k0 = k0_first;
+                    nk = nk_first;
+                    inc = inc_first;
+                } else {
+                    k0 = W.item_k0[i];
+                    nk = W.item_nk[i];
+                    inc = W.item_inc[i];
+                }
+            }
             uint32_t tot = 0;
             const uint32_t ex = block_excl_scan(nk, s_tmp, &tot);
-            if (nk) {
-                const int64_t k0 = W.item_k0[i];
-                const uint32_t inc = W.item_inc[i];
-                for (uint32_t j = 0; j < nk; ++j) {
-                    const int64_t u = base + ex + j, key = k0 + j;
-                    if (!GG_OK(u, W.units_cap, 14)) break;
-                    const int64_t a = ix.codec ? ix.key_seg[key] : ix.key_off[key];
-                    const int64_t e = ix.codec ? ix.key_seg[key + 1] : ix.key_off[key + 1];
-                    W.span_start[u] = a;
-                    W.span_len[u] = e - a;
-                    W.inc[u] = inc;
+            if (c == i0 && nk == 1 && !ix.codec) {      // a single list: its offsets are at hand
+                if (GG_OK(base + ex, W.units_cap, 14)) {
+                    W.span_start[base + ex] = a_first;
+                    W.span_len[base + ex] = e_first - a_first;
+                    W.inc[base + ex] = inc;
                 }
+                nk = 0;
+            }
+            for (uint32_t j = 0; j < nk; ++j) {
+                const int64_t u = base + ex + j, key = k0 + j;
+                if (!GG_OK(u, W.units_cap, 14)) break;
+                const int64_t a = ix.codec ? ix.key_seg[key] : ix.key_off[key];
+                const int64_t e = ix.codec ? ix.key_seg[key + 1] : ix.key_off[key + 1];
+                W.span_start[u] = a;
+                W.span_len[u] = e - a;
+                W.inc[u] = inc;
             }
             base += tot;
         }
     }
+    QInfo qi;
+    qi.total = (int64_t)total;
+    qi.unit0 = unit0;
+    qi.n_units = (int32_t)n_units;
+    qi.item0 = i0;
+    qi.n_items = m;
+    qi.k = k;
+    qi.scale = scale;
+    qi.flags = weighted ? kFlagWeighted : 0;
+    // bound on any object's count: one match per item on a one-value-per-dim
+    // table; on a bag table, every covered list may repeat the object
+    const int64_t bound = ix.is_bag ? n_units * ix.mult_max : (int64_t)m;
+    if (!weighted && bound <= 255) qi.flags |= kFlagSmallCount;
+    qi.parts = 1;
+    qi.cls = kClsNone;
     if (tid == 0) {
-        const uint32_t k = qi.k;
+        W.done[q] = 0;
+        W.qstate[q] = 0;
+        if (k == 0 || k > (uint32_t)kMaxK) atomicOr(&W.ctr[kCtrError], kErrCapacity);
         const bool small = (qi.flags & kFlagSmallCount) != 0;
         const int64_t total = qi.total;
         int list = -1;
@@ -982,9 +999,8 @@ Tuning launch_tuning(const DevIndex &ix, const Tuning &tun, int num_sms) {
 
 int launch_plan(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t, cudaStream_t s) {
     cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(uint32_t), s);
-    k_plan_items<<<Q.n_queries, kPlanThreads, 0, s>>>(ix, Q, W, t);
-    k_plan_units<<<Q.n_queries, kPlanThreads, 0, s>>>(ix, Q, W, t);
-    return 2;
+    k_plan<<<Q.n_queries, kPlanThreads, 0, s>>>(ix, Q, W, t);
+    return 1;
 }
 
 // One match kernel (kListBitmap .. kListDenseWide) as a persistent grid.

@@ -36,7 +36,7 @@ def test_graph_batch_varying_sizes(genie, oracle):
         pid, pcnt = genie.search(t, qb)
         assert np.array_equal(ids, pid) and np.array_equal(cnt, pcnt)
     kernels, ms = bt.last_stats()
-    assert kernels >= 7 and ms > 0
+    assert kernels >= 6 and ms > 0      # the plan, then one kernel per work list
 
 
 def test_stage_launch_fetch_repeatable(genie, oracle):
