@@ -57,6 +57,9 @@ def parse():
     p.add_argument("--serve-objects", type=int, default=1_000_000,
                    help="objects of the config2/config3 indexes resident beside config1 while serving")
     p.add_argument("--serve-seconds", type=float, default=0.2, help="arrival window per offered rate")
+    p.add_argument("--profile-batch", type=int, default=0,
+                   help="only run the workload's batch this many times without a graph (for ncu), print its "
+                        "per-kernel times and exit")
     p.add_argument("--tuning", default="",
                    help="fixed kernel shape, e.g. sparse_slots=53248,sparse_ctas_per_sm=1 (skips autotuning)")
     return p.parse_args()
@@ -71,7 +74,7 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel):
+def ncu_traffic(kernel, workload):
     """traffic_bytes_per_launch recorded in profiles/ for this kernel/workload."""
     pdir = os.path.join(ROOT, "profiles")
     if not os.path.isdir(pdir):
@@ -81,7 +84,7 @@ def ncu_traffic(kernel):
             continue
         with open(os.path.join(pdir, name)) as f:
             txt = f.read()
-        if "workload: config1" not in txt or ("kernel: " + kernel) not in txt:
+        if ("workload: " + workload) not in txt or ("kernel: " + kernel) not in txt:
             continue
         m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
         if m:
@@ -334,6 +337,17 @@ def main():
     n_items = int(batch["item_off"][-1])
     Q = qb.n_queries
     max_k = int(np.max(batch["k"]))
+    if args.profile_batch:
+        bp = g.Batch(table, Q, n_items, max_k, use_graph=False)
+        if args.tuning:
+            bp.set_tuning(**{kv.split("=")[0]: int(kv.split("=")[1]) for kv in args.tuning.split(",")})
+        bp.stage(qb)
+        for _ in range(args.profile_batch):
+            bp.launch()
+            bp.fetch()
+        print(json.dumps({"profile_batch": args.profile_batch, "workload": args.workload,
+                          "stage_ms": [round(float(x), 4) for x in bp.stage_ms()]}))
+        return
 
     # one non-default stream carries the L2 flushes, the events and the graph
     # launches (a null handle would select the batch's own stream instead)
@@ -410,7 +424,7 @@ def main():
     dom_ms = float(sum(stage_tot[i] for i in busy)) / args.steps
     peak, peak_kind = peaks()
     achieved = alg_bytes / (dom_ms / 1e3) / 1e9
-    traffic = ncu_traffic(names[dom]) if len(busy) == 1 else None
+    traffic = ncu_traffic(names[dom], args.workload) if len(busy) == 1 else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": "+".join(names[i] for i in busy), "kernel_ms": dom_ms,
                 "algorithmic_bytes_per_launch": alg_bytes, "peak_source": peak_kind,
