@@ -429,6 +429,49 @@ __device__ __forceinline__ void stream_units(const DevIndex &ix, const ItemStage
     else stream_ids1(ix.ids, ix.n_ids, st, n_items, F, visit);
 }
 
+// Plain lists in long runs (the dense kernel): warp tasks of kRun consecutive
+// posting positions of one staged sub-span.  st.flat holds the exclusive
+// prefix of the sub-spans' task counts, st.len their lengths.  The item
+// lookup happens once per task instead of once per id, and a lane's loads
+// are immediate offsets from one pointer, so the per-id work is the load and
+// visit(id, inc).
+constexpr uint32_t kRun = 1024;
+template <class V>
+__device__ __forceinline__ void stream_runs(const uint32_t *__restrict__ ids, const ItemStage &st, uint32_t n_items,
+                                            uint32_t n_tasks, V &&visit) {
+    constexpr int R = 16;                 // loads in flight per lane
+    const uint32_t lane = lane_id(), nw = blockDim.x >> 5;
+    for (uint32_t f = warp_id(); f < n_tasks; f += nw) {
+        uint32_t a = 0, b = n_items;      // last sub-span with flat <= f
+        while (a < b) {
+            const uint32_t mid = (a + b + 1) >> 1;
+            if (st.flat[mid] <= f) a = mid; else b = mid - 1;
+        }
+        const uint32_t r0 = (f - st.flat[a]) * kRun;
+        const uint32_t n = min(kRun, st.len[a] - r0);
+        const uint32_t inc = st.inc[a];
+        const uint32_t *p = ids + st.start[a] + r0 + lane;
+        if (n == kRun) {
+            for (uint32_t g = 0; g < kRun / 32; g += R) {
+                uint32_t v[R];
+#pragma unroll
+                for (int r = 0; r < R; ++r) v[r] = __ldg(p + 32 * (g + r));
+#pragma unroll
+                for (int r = 0; r < R; ++r) visit(v[r], inc);
+            }
+        } else {
+            for (uint32_t g = 0; 32 * g < n; g += R) {
+                uint32_t v[R];
+#pragma unroll
+                for (int r = 0; r < R; ++r) v[r] = 32 * (g + r) + lane < n ? __ldg(p + 32 * (g + r)) : 0u;
+#pragma unroll
+                for (int r = 0; r < R; ++r)
+                    if (32 * (g + r) + lane < n) visit(v[r], inc);
+            }
+        }
+    }
+}
+
 // First unit (posting position, or segment of a compressed index) of the
 // range [s0, e0) that can hold an id >= x.
 __device__ __forceinline__ int64_t first_unit(const DevIndex &ix, int64_t s0, int64_t e0, uint32_t x) {
@@ -861,24 +904,33 @@ __global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Wo
                     st.start[tid] = a;
                     st.inc[tid] = W.inc[it];
                     len = (uint32_t)(b - a);
+                    st.len[tid] = len;
                     // a compressed segment may straddle tile_hi: the next tile starts at it again
                     if (single) cur[tid] = (ix.codec && b > a) ? b - 1 : b;
                 }
+                // plain lists go by warp tasks of kRun positions; segments one per warp
+                const uint32_t units = ix.codec ? len : (len + kRun - 1) / kRun;
                 uint32_t tot = 0;
-                uint32_t off = block_excl_scan(len, ss.tmp, &tot);
+                uint32_t off = block_excl_scan(units, ss.tmp, &tot);
                 if ((int32_t)tid < mc) st.flat[tid] = off;
                 if (tid == 0) st.flat[mc] = tot;
                 __syncthreads();
                 if (tot) any_ids = true;
                 if (SMALL) {
-                    stream_units(ix, st, (uint32_t)mc, tot, tile_lo, tile_hi, [&](uint32_t id, uint32_t) {
+                    // byte counters, four to a word: the word at loc & ~3, the byte (loc & 3)
+                    auto add = [&](uint32_t id, uint32_t) {
                         const uint32_t loc = id - tile_lo;
-                        if (GG_OK(loc, n_ids, 3)) atomicAdd(&cnt[loc >> 2], 1u << ((loc & 3u) << 3));
-                    });
+                        if (GG_OK(loc, n_ids, 3))
+                            atomicAdd((uint32_t *)((unsigned char *)cnt + (loc & ~3u)), __funnelshift_l(0u, 1u, loc << 3));
+                    };
+                    if (ix.codec) stream_segments(ix, st, (uint32_t)mc, tot, tile_lo, tile_hi, add);
+                    else stream_runs(ix.ids, st, (uint32_t)mc, tot, add);
                 } else {
-                    stream_units(ix, st, (uint32_t)mc, tot, tile_lo, tile_hi, [&](uint32_t id, uint32_t inc) {
+                    auto add = [&](uint32_t id, uint32_t inc) {
                         if (GG_OK(id - tile_lo, n_ids, 3)) atomicAdd(&cnt[id - tile_lo], inc);
-                    });
+                    };
+                    if (ix.codec) stream_segments(ix, st, (uint32_t)mc, tot, tile_lo, tile_hi, add);
+                    else stream_runs(ix.ids, st, (uint32_t)mc, tot, add);
                 }
                 __syncthreads();
             }
