@@ -185,6 +185,46 @@ __device__ __forceinline__ int64_t gallop_u32(const uint32_t *__restrict__ a, in
     }
 }
 
+// First position p in [lo, hi) with a[p] >= x (hi if none), a sorted, by
+// 8-way probes: every step issues 8 independent loads and keeps the
+// sub-range between the last probe below x and the first at or above it.
+// The first step centres its probes on `guess` at a spacing of `win` (an
+// estimate of the answer and of its error), later steps split the range
+// evenly, so a good guess needs ~3 dependent steps instead of the ~2 log2(n)
+// of a galloping search.
+__device__ __forceinline__ int64_t probe8_first_ge(const uint32_t *__restrict__ a, int64_t lo, int64_t hi,
+                                                   uint32_t x, int64_t guess, int64_t win) {
+    int64_t L = lo, H = hi;          // the answer lies in [L, H]
+    bool first = true;
+    while (H - L > 8) {
+        // probe offsets from L (a list holds < 2^32 ids)
+        const uint32_t n = (uint32_t)(H - L);
+        const int64_t c = guess - L;
+        uint32_t off[8], v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            int64_t q = first ? c + (int64_t)(j - 4) * win : (int64_t)(((uint64_t)n * (j + 1)) / 9);
+            off[j] = (uint32_t)(q < 0 ? 0 : (q > (int64_t)n - 1 ? (int64_t)n - 1 : q));
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) v[j] = __ldg(a + L + off[j]);
+        uint32_t nl = 0, nh = n;      // new range [L + nl, L + nh]
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (v[j] < x) nl = max(nl, off[j] + 1);
+            else nh = min(nh, off[j]);
+        }
+        H = L + nh;
+        L = L + min(nl, nh);
+        first = false;
+    }
+    uint32_t below = 0;      // the last <= 8 positions, loaded together
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (L + j < H && __ldg(a + L + j) < x) ++below;
+    return L + below;
+}
+
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {

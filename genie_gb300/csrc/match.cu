@@ -472,6 +472,31 @@ __device__ __forceinline__ void stream_runs(const uint32_t *__restrict__ ids, co
     }
 }
 
+// Searches in a sorted list [s0, e0) over ids [0, N) (or its segments' first
+// ids) that start at the position the list's density predicts: ids of a list
+// are spread over the id space, so the error is about the square root of the
+// count, and an 8-way probe search (probe8_first_ge) needs a few steps.
+__device__ __forceinline__ int64_t near_win(int64_t expect) {
+    int64_t w = 4;
+    while (w * w < expect) w <<= 1;
+    return w;
+}
+// First unit of [s0, e0) that can hold an id >= x.
+__device__ __forceinline__ int64_t first_unit_near(const DevIndex &ix, int64_t s0, int64_t e0, uint32_t x, uint64_t N) {
+    const int64_t len = e0 - s0, expect = (int64_t)((double)len * x / (double)N);
+    const int64_t w = near_win(expect) / 2;
+    if (!ix.codec) return probe8_first_ge(ix.ids, s0, e0, x, s0 + expect, w);
+    const int64_t a = probe8_first_ge(ix.seg_first, s0, e0, x, s0 + expect, w);
+    return a > s0 ? a - 1 : a;
+}
+// From a (the tile's first unit), the first unit holding ids >= hi (for a
+// compressed index: the first segment starting at >= hi).
+__device__ __forceinline__ int64_t next_unit_near(const DevIndex &ix, int64_t a, int64_t s0, int64_t e0, uint32_t lo,
+                                                  uint32_t hi, uint64_t N) {
+    const int64_t expect = (int64_t)((double)(e0 - s0) * (hi - lo) / (double)N);
+    return probe8_first_ge(ix.codec ? ix.seg_first : ix.ids, a, e0, hi, a + expect, near_win(expect) / 2);
+}
+
 // First unit (posting position, or segment of a compressed index) of the
 // range [s0, e0) that can hold an id >= x.
 __device__ __forceinline__ int64_t first_unit(const DevIndex &ix, int64_t s0, int64_t e0, uint32_t x) {
@@ -856,7 +881,7 @@ __global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Wo
     st.inc = (uint32_t *)(it_raw + kItemChunk * 20);
     st.flat = (uint32_t *)(it_raw + kItemChunk * 24);
     SelectScratch &ss = *(SelectScratch *)(it_raw + kItemChunk * 28 + 16);
-    __shared__ uint32_t s_work, s_nS;
+    __shared__ uint32_t s_work, s_nS, s_nc;
 
     const int list = SMALL ? kListDenseSmall : kListDenseWide;
     for (;;) {
@@ -880,7 +905,7 @@ __global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Wo
         if (single && (int32_t)tid < qi.n_units) {
             const int64_t it = qi.unit0 + tid;
             const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
-            cur[tid] = (t0 == 0 || e0 == s0) ? s0 : first_unit(ix, s0, e0, (uint32_t)(t0 * tile_cap));
+            cur[tid] = (t0 == 0 || e0 == s0) ? s0 : first_unit_near(ix, s0, e0, (uint32_t)(t0 * tile_cap), N);
         }
         __syncthreads();
         for (uint64_t t = t0; t < t1; ++t) {
@@ -900,7 +925,7 @@ __global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Wo
                     const int64_t it = qi.unit0 + c0 + tid;
                     const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
                     int64_t a = single ? cur[tid] : (t == 0 ? s0 : first_unit(ix, s0, e0, tile_lo));
-                    int64_t b = (tile_hi >= N) ? e0 : gallop_u32(ix.codec ? ix.seg_first : ix.ids, a, e0, tile_hi);
+                    int64_t b = (tile_hi >= N) ? e0 : next_unit_near(ix, a, s0, e0, tile_lo, tile_hi, N);
                     st.start[tid] = a;
                     st.inc[tid] = W.inc[it];
                     len = (uint32_t)(b - a);
@@ -938,6 +963,54 @@ __global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Wo
             // merge this tile into the running top-k
             const uint32_t nS = s_nS;
             const uint32_t thr = nS == qi.k ? key_prim(S[qi.k - 1]) : 0u;
+            if (nS == qi.k) {
+                // S is full: a tile id enters only with a count above S's k-th
+                // (on a tie S's id, from an earlier tile, is smaller).  Few
+                // counters usually are: collect them behind a copy of S and
+                // sort the union.
+                if (tid == 0) s_nc = 0;
+                for (uint32_t i = tid; i < nS; i += blockDim.x) cand[i] = S[i];
+                __syncthreads();
+                const uint32_t room = (uint32_t)kCandCap - nS;
+                const uint32_t per = SMALL ? 16u : 4u;
+                const uint32_t nvec = (n_ids + per - 1) / per;
+                const uint32_t thr4 = SMALL ? thr * 0x01010101u : thr;
+                for (uint32_t b = 0; b < nvec; b += blockDim.x) {
+                    const uint32_t v = b + tid;
+                    const bool act = v < nvec;
+                    const uint4 w = act ? ((const uint4 *)cnt)[v] : make_uint4(0, 0, 0, 0);
+                    bool any;
+                    if (SMALL)
+                        any = (__vcmpgtu4(w.x, thr4) | __vcmpgtu4(w.y, thr4) | __vcmpgtu4(w.z, thr4) |
+                               __vcmpgtu4(w.w, thr4)) != 0u;
+                    else
+                        any = w.x > thr || w.y > thr || w.z > thr || w.w > thr;
+                    if (__ballot_sync(0xffffffffu, act && any) == 0u) continue;
+                    const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+                    for (uint32_t e = 0; e < per; ++e) {
+                        const uint32_t prim = SMALL ? ((words[e >> 2] >> ((e & 3) * 8)) & 255u) : words[e];
+                        const uint32_t local = v * per + e;
+                        const bool keep = act && prim > thr && local < n_ids;
+                        const uint32_t mk = __ballot_sync(0xffffffffu, keep);
+                        if (!mk) continue;
+                        uint32_t at = 0;
+                        if (lane_id() == 0) at = atomicAdd(&s_nc, (uint32_t)__popc(mk));
+                        at = __shfl_sync(0xffffffffu, at, 0) + (uint32_t)__popc(mk & ((1u << lane_id()) - 1u));
+                        if (keep && at < room) cand[nS + at] = make_key(prim, tile_lo + local);
+                    }
+                }
+                __syncthreads();
+                const uint32_t m = s_nc;
+                if (m <= room) {
+                    const uint32_t np2 = next_pow2(nS + m);
+                    for (uint32_t i = nS + m + tid; i < np2; i += blockDim.x) cand[i] = 0ull;
+                    bitonic_sort_desc(cand, np2);
+                    for (uint32_t i = tid; i < nS; i += blockDim.x) S[i] = cand[i];
+                    __syncthreads();
+                    continue;
+                }
+            }
             TileSet<SMALL> ts{cnt, n_ids, tile_lo, thr, S, nS};
             const uint32_t nn = select_topk(ts, qi.k, SMALL ? 8 : 32, cand, kCandCap, ss);
             for (uint32_t i = tid; i < nn; i += blockDim.x)
