@@ -408,14 +408,14 @@ def main():
     bp = g.Batch(table, Q, n_items, max_k, use_graph=False)
     bp.set_tuning(**{k: v for k, v in tuning.items()})
     bp.stage(qb)
-    stage_tot = np.zeros(6)
+    stage_tot = np.zeros(4)
     for i in range(args.warmup + args.steps):
         flush.zero_()
         bp.launch(stream.cuda_stream)
         ms = bp.stage_ms()
         if i >= args.warmup:
             stage_tot += ms
-    names = ["k_plan", "k_bitmap", "k_sparse<packed>", "k_sparse<wide>", "k_dense<u8>", "k_dense<u32>"]
+    names = ["k_plan", "k_bitmap", "k_sparse", "k_dense"]
     # the match kernels that carry the batch (>= 15% of the match time); when
     # several share it, their posting bytes are counted over their summed time
     match_ms = stage_tot[1:]

@@ -85,9 +85,9 @@ class Batch:
 
     def stage_ms(self):
         """Per-stage device ms of the last launch (batches made with use_graph=False):
-        plan, bitmap, sparse-packed, sparse-wide, dense-small, dense-wide."""
+        plan, bitmap, sparse (both slot widths), dense (both counter widths)."""
         from . import _check, lib
-        ms = np.zeros(6, np.float32)
+        ms = np.zeros(4, np.float32)
         _check(lib().genie_batch_stage_ms(self._h, ms.ctypes.data))
         return ms
 

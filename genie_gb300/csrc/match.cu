@@ -667,7 +667,7 @@ struct HashSet {
 // NT = 512: two CTAs per SM with mid-size tables; NT = 1024: one CTA per SM
 // with the largest table, so a query needs fewer id-range parts.
 template <bool PACKED, int NT>
-__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_sparse(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+__device__ __forceinline__ void sparse_list(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &T) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t tid = threadIdx.x;
     const uint32_t slots_max = PACKED ? (uint32_t)T.sparse_slots_packed : (uint32_t)T.sparse_slots_wide;
@@ -809,6 +809,15 @@ __global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_sparse(DevIndex ix, D
     }
 }
 
+// Both sparse work lists in one launch (their tables take the same shared
+// memory): the 4-byte-slot list, then the 8-byte-slot list.  Each list is
+// drained before the next; a launch whose lists are empty costs one check.
+template <int NT>
+__global__ void __launch_bounds__(NT, NT == 512 ? 2 : 1) k_sparse(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+    sparse_list<true, NT>(ix, Q, W, T);
+    sparse_list<false, NT>(ix, Q, W, T);
+}
+
 // ------------------------------------------------------------------ bitmap
 
 }  // namespace gg
@@ -865,7 +874,7 @@ struct TileSet {
 // (match.cu:276-294, match_device_utils.h:422-446), which wraps above
 // 2^bits - 1; these counters are sized from the item count and never wrap.
 template <bool SMALL>
-__global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+__device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &T) {
     extern __shared__ __align__(16) unsigned char smem[];
     const uint32_t tid = threadIdx.x;
     const uint32_t tile_cap = SMALL ? (uint32_t)T.dense_tile_u8 : (uint32_t)T.dense_tile_u32;
@@ -1027,6 +1036,13 @@ __global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Wo
     }
 }
 
+// Both dense work lists in one launch (1-byte and 4-byte counter tiles take
+// the same shared memory), one after the other.
+__global__ void __launch_bounds__(1024, 1) k_dense(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+    dense_list<true>(ix, Q, W, T);
+    dense_list<false>(ix, Q, W, T);
+}
+
 // ------------------------------------------------------------------ host side
 
 size_t sparse_smem_bytes(const Tuning &t, bool packed) {
@@ -1063,14 +1079,14 @@ static cudaError_t set_smem(const void *fn, size_t bytes) {
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
+size_t sparse_smem_both(const Tuning &t) { return std::max(sparse_smem_bytes(t, true), sparse_smem_bytes(t, false)); }
+size_t dense_smem_both(const Tuning &t) { return std::max(dense_smem_bytes(t, true), dense_smem_bytes(t, false)); }
+
 cudaError_t prepare_kernels(const Tuning &t) {
     cudaError_t e;
-    if ((e = set_smem((const void *)k_sparse<true, 512>, sparse_smem_bytes(t, true)))) return e;
-    if ((e = set_smem((const void *)k_sparse<false, 512>, sparse_smem_bytes(t, false)))) return e;
-    if ((e = set_smem((const void *)k_sparse<true, 1024>, sparse_smem_bytes(t, true)))) return e;
-    if ((e = set_smem((const void *)k_sparse<false, 1024>, sparse_smem_bytes(t, false)))) return e;
-    if ((e = set_smem((const void *)k_dense<true>, dense_smem_bytes(t, true)))) return e;
-    if ((e = set_smem((const void *)k_dense<false>, dense_smem_bytes(t, false)))) return e;
+    if ((e = set_smem((const void *)k_sparse<512>, sparse_smem_both(t)))) return e;
+    if ((e = set_smem((const void *)k_sparse<1024>, sparse_smem_both(t)))) return e;
+    if ((e = set_smem((const void *)k_dense, dense_smem_both(t)))) return e;
     return cudaSuccess;
 }
 
@@ -1079,9 +1095,8 @@ cudaError_t prepare_kernels_max() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if (optin <= 0) optin = 227 * 1024;
-    const void *fns[] = {(const void *)k_sparse<true, 512>, (const void *)k_sparse<false, 512>,
-                         (const void *)k_sparse<true, 1024>, (const void *)k_sparse<false, 1024>,
-                         (const void *)k_dense<true>, (const void *)k_dense<false>, (const void *)k_bitmap};
+    const void *fns[] = {(const void *)k_sparse<512>, (const void *)k_sparse<1024>, (const void *)k_dense,
+                         (const void *)k_bitmap};
     for (const void *fn : fns) {
         cudaFuncAttributes a;
         cudaError_t e = cudaFuncGetAttributes(&a, fn);
@@ -1128,43 +1143,33 @@ int launch_plan(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tu
     return 1;
 }
 
-// One match kernel (kListBitmap .. kListDenseWide) as a persistent grid.
-int launch_list(int list, const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t, int num_sms,
-                cudaStream_t s) {
+// The match kernels as persistent grids: the bitmap kernel, the sparse
+// kernel (both slot widths), the dense kernel (both counter widths).
+enum : int { kKernBitmap = 0, kKernSparse = 1, kKernDense = 2, kNumKern = 3 };
+int launch_kernel(int kern, const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t, int num_sms,
+                  cudaStream_t s) {
     // persistent grids: as many CTAs as fit on every SM at once
     auto grid = [&](const void *fn, int threads, size_t smem) {
         int per_sm = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
         return num_sms * std::max(1, per_sm);
     };
-    const bool wide_ctas = t.sparse_threads == 1024;
-    switch (list) {
-    case kListBitmap: {
+    switch (kern) {
+    case kKernBitmap: {
         if (t.bitmap_bits <= 0) return 0;
         const size_t bp = bm_layout(ix.n_objects, (uint32_t)t.bitmap_multi_slots).bytes;
         k_bitmap<<<num_sms, kBmThreads, bp, s>>>(ix, Q, W, t);
         return 1;
     }
-    case kListSparsePacked: {
-        const size_t sp = sparse_smem_bytes(t, true);
-        if (wide_ctas) k_sparse<true, 1024><<<grid((const void *)k_sparse<true, 1024>, 1024, sp), 1024, sp, s>>>(ix, Q, W, t);
-        else k_sparse<true, 512><<<grid((const void *)k_sparse<true, 512>, 512, sp), 512, sp, s>>>(ix, Q, W, t);
-        return 1;
-    }
-    case kListSparseWide: {
-        const size_t sw = sparse_smem_bytes(t, false);
-        if (wide_ctas) k_sparse<false, 1024><<<grid((const void *)k_sparse<false, 1024>, 1024, sw), 1024, sw, s>>>(ix, Q, W, t);
-        else k_sparse<false, 512><<<grid((const void *)k_sparse<false, 512>, 512, sw), 512, sw, s>>>(ix, Q, W, t);
-        return 1;
-    }
-    case kListDenseSmall: {
-        const size_t dp = dense_smem_bytes(t, true);
-        k_dense<true><<<grid((const void *)k_dense<true>, t.dense_threads, dp), t.dense_threads, dp, s>>>(ix, Q, W, t);
+    case kKernSparse: {
+        const size_t sp = sparse_smem_both(t);
+        if (t.sparse_threads == 1024) k_sparse<1024><<<grid((const void *)k_sparse<1024>, 1024, sp), 1024, sp, s>>>(ix, Q, W, t);
+        else k_sparse<512><<<grid((const void *)k_sparse<512>, 512, sp), 512, sp, s>>>(ix, Q, W, t);
         return 1;
     }
     default: {
-        const size_t dw = dense_smem_bytes(t, false);
-        k_dense<false><<<grid((const void *)k_dense<false>, t.dense_threads, dw), t.dense_threads, dw, s>>>(ix, Q, W, t);
+        const size_t dp = dense_smem_both(t);
+        k_dense<<<grid((const void *)k_dense, t.dense_threads, dp), t.dense_threads, dp, s>>>(ix, Q, W, t);
         return 1;
     }
     }
@@ -1178,10 +1183,10 @@ int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const T
     if (ev) cudaEventRecord(ev[0], s);
     launches += launch_plan(ix, Q, W, t, s);
     if (ev) cudaEventRecord(ev[1], s);
-    const int order[kNumLists] = {kListBitmap, kListSparsePacked, kListSparseWide, kListDenseSmall, kListDenseWide};
-    for (int i = 0; i < kNumLists; ++i) {
-        launches += launch_list(order[i], ix, Q, W, t, num_sms, s);
-        if (ev) cudaEventRecord(ev[2 + i], s);
+    // dense last: sparse parts that overflow are re-queued to the dense lists
+    for (int k = 0; k < kNumKern; ++k) {
+        launches += launch_kernel(k, ix, Q, W, t, num_sms, s);
+        if (ev) cudaEventRecord(ev[2 + k], s);
     }
     return launches;
 }

@@ -16,12 +16,12 @@ cudaError_t prepare_kernels(const Tuning &t);
 // Allow the largest dynamic shared memory on every match kernel (once per device).
 cudaError_t prepare_kernels_max();
 
-// Enqueue plan + sparse + dense kernels for one batch on stream s.  All
-// pointers in Q and W are device pointers; W arrays are sized for Q.
-// Returns the number of kernel launches issued.  With `ev` (7 events), event
-// i+1 is recorded after stage i: plan, bitmap, sparse-packed, sparse-wide,
-// dense-small, dense-wide (event 0 before the plan).
-constexpr int kStages = 6;
+// Enqueue plan + bitmap + sparse + dense kernels for one batch on stream s.
+// All pointers in Q and W are device pointers; W arrays are sized for Q.
+// Returns the number of kernel launches issued.  With `ev` (5 events), event
+// i+1 is recorded after stage i: plan, bitmap, sparse (both slot widths),
+// dense (both counter widths); event 0 before the plan.
+constexpr int kStages = 4;
 // Whether the bitmap kernel's shared memory fits an id space of n objects.
 bool bitmap_fits(const Tuning &t, int64_t n_objects);
 int launch_match(const DevIndex &ix, const DevQueries &Q, const Work &W, const Tuning &t,

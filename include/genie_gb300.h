@@ -238,8 +238,8 @@ int genie_batch_set_tuning(genie_batch *b, const genie_tuning *t);
 int genie_batch_last_stats(const genie_batch *b, int32_t *kernels, float *device_ms);
 /* Device milliseconds of each stage of the last launch of a batch created
  * with use_graph = 0: ms[0] plan (+ counter reset), ms[1] presence-bitmap
- * kernel, ms[2] sparse 4-byte-slot kernel, ms[3] sparse 8-byte-slot kernel,
- * ms[4] dense 1-byte-counter kernel, ms[5] dense 4-byte-counter kernel. */
+ * kernel, ms[2] sparse kernel (4- and 8-byte slots), ms[3] dense kernel
+ * (1- and 4-byte counters). */
 int genie_batch_stage_ms(const genie_batch *b, float *ms);
 
 /* ---------------------------------------------------------------- serving */
