@@ -34,7 +34,14 @@
 namespace gg {
 
 constexpr uint32_t kBmThreads = 1024;
-constexpr uint32_t kBmChunks = 4096;      // 32-id chunks per query on this path
+constexpr uint32_t kBmChunks = 2048;      // 32-id chunks per query on this path
+// selection buffers of a query with >= k table entries, over the bitmap (which
+// nothing reads then): candidate keys, tie ids, tie keys, bucket counters
+constexpr uint32_t kBmScrTieIds = kCandCap * 8;
+constexpr uint32_t kBmScrTieKeys = kBmScrTieIds + kCandCap * 4;
+constexpr uint32_t kBmScrBuckets = kBmScrTieKeys + kCandCap / 2 * 8;
+constexpr uint32_t kBmScratch = kBmScrBuckets + 1024 * 4;
+static_assert(kBmChunks >= (uint32_t)kMaxK, "the chunk region holds the keys of a query with < k table entries");
 constexpr uint32_t kBmProbe = 128;        // longest probe run of the repeated-id table
 constexpr int kBmRound = 16;              // chunk loads in flight per lane
 constexpr uint32_t kBmDescRing = 128;     // query descriptors kept in shared memory
@@ -49,10 +56,10 @@ __host__ __device__ inline BmLayout bm_layout(int64_t n_objects, uint32_t mslots
     BmLayout L;
     uint32_t o = 0;
     L.bm_words = (uint32_t)((n_objects + 127) / 128) * 4;
-    L.bm = o;     o += bm_align(L.bm_words * 4, 128);
+    L.bm = o;     o += bm_align(L.bm_words * 4 > kBmScratch ? L.bm_words * 4 : kBmScratch, 128);
     L.mt = o;     o += bm_align(mslots * 4, 128);
     L.mlist = o;  o += bm_align(mslots / 2 * 4, 128);     // slots of the table's entries
-    L.chunk = o;  o += kBmChunks * 8;      // also the candidate keys after streaming
+    L.chunk = o;  o += kBmChunks * 8;      // also the result keys of a query with < k table entries
     L.ss = o;     o += bm_align((uint32_t)sizeof(SelectScratch), 16);
     L.bytes = bm_align(o, 128);
     return L;
@@ -140,9 +147,10 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
     // empty entry (0, 0) reads ids [0, 32) and counts none of them
     uint2 *chunk = (uint2 *)(smem + L.chunk);
     uint32_t *mlist = (uint32_t *)(smem + L.mlist);
-    uint64_t *cand = (uint64_t *)(smem + L.chunk);                  // [0, kCandCap)
-    uint32_t *tie_ids = (uint32_t *)(cand + kCandCap);               // [0, kCandCap)
-    uint64_t *tie_keys = cand + kCandCap + kCandCap / 2;             // [0, kCandCap / 2)
+    uint64_t *cand_few = (uint64_t *)(smem + L.chunk);                    // [0, kMaxK)
+    uint64_t *cand_s = (uint64_t *)(smem + L.bm);                         // [0, kCandCap)
+    uint32_t *tie_ids = (uint32_t *)(smem + L.bm + kBmScrTieIds);         // [0, kCandCap)
+    uint64_t *tie_keys = (uint64_t *)(smem + L.bm + kBmScrTieKeys);       // [0, kCandCap / 2)
     SelectScratch &ss = *(SelectScratch *)(smem + L.ss);
     uint32_t *hist = ss.hist;
     __shared__ uint32_t s_multi, s_ovf, s_n, s_big;
@@ -297,14 +305,16 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
         const bool ovf = s_ovf != 0;
         bool failed = ovf || n_chunks > kBmChunks;
         uint32_t nres = 0, n_hi = 0, cstar = 0;     // keys cand[0, n_hi), then tie ids at c*
+        uint64_t *cand = cand_few;
         if (!failed && n_multi >= k) {
+            cand = cand_s;
             // tie ids go to id-range buckets (counting sort): bucket b holds ids
-            // [b << sh, (b+1) << sh); the counters borrow the first bitmap
-            // words, cleared while warp 0 finds c*
+            // [b << sh, (b+1) << sh); the counters, cleared while warp 0 finds
+            // c*, and these buffers lie over the bitmap
             const uint32_t nb = min(1024u, words);
             uint32_t sh = 0;
             while (((uint32_t)(ix.n_objects - 1) >> sh) >= nb) ++sh;
-            uint32_t *bcnt = bm;
+            uint32_t *bcnt = (uint32_t *)((unsigned char *)bm + kBmScrBuckets);
             for (uint32_t x = tid; x < nb; x += kBmThreads) bcnt[x] = 0u;
             if (warp == 0) find_digit(ss, k, true);     // k-th largest count
             if (tid == 0) {

@@ -26,7 +26,7 @@ enum : uint8_t { kFlagWeighted = 1, kFlagSmallCount = 2, kFlagRetry = 4, kFlagPa
 // posting lists a query may cover on the bitmap path (one per thread)
 constexpr uint32_t kBmSpanCap = 1024;
 // posting ids of a query on the bitmap path (its 32-id chunk entries)
-constexpr uint32_t kBmMaxIds = 96 * 1024;
+constexpr uint32_t kBmMaxIds = 40 * 1024;
 // zero bytes behind the posting ids of a plain index: 32 ids read from the
 // last position stay inside the allocation
 constexpr size_t kIdsPadBytes = 128;

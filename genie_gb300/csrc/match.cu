@@ -1070,7 +1070,7 @@ Tuning default_tuning() {
     t.dense_ctas_per_sm = 1;
     t.sparse_load_pct = 50;
     t.bitmap_bits = 1179648;         // id spaces up to 144 KiB of presence bits
-    t.bitmap_multi_slots = 4096;     // 16 KiB table of repeated ids
+    t.bitmap_multi_slots = 2048;     // 8 KiB table of repeated ids
     t.bitmap_ready = 0;              // set per launch
     return t;
 }
