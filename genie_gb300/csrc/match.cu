@@ -553,6 +553,18 @@ __device__ uint64_t stage_range(const DevIndex &ix, const Work &W, const QInfo &
     return r;
 }
 
+// Next item of a work list for this CTA, or ~0 when the list is done.  The
+// list's count is fixed while its kernel runs (re-queued work goes to a list
+// of a later kernel).  The count is read first, so a CTA that finds the list
+// empty or drained takes no atomic: an empty list costs every CTA one read
+// instead of an atomic on the counter all CTAs share.
+__device__ __forceinline__ uint32_t take_work(const Work &W, int list) {
+    const uint32_t n = *(volatile uint32_t *)&W.ctr[2 * list];
+    if (*(volatile uint32_t *)&W.ctr[2 * list + 1] >= n) return 0xFFFFFFFFu;
+    const uint32_t w = atomicAdd(&W.ctr[2 * list + 1], 1u);
+    return w < n ? w : 0xFFFFFFFFu;
+}
+
 // Scratch / merge of a query's parts.  Part p of query q keeps its sorted
 // top-k keys in scratch[out_off*kMaxParts + p*k ..].
 struct MergeSet {
@@ -688,11 +700,11 @@ __device__ __forceinline__ void sparse_list(const DevIndex &ix, const DevQueries
 
     const int list = PACKED ? kListSparsePacked : kListSparseWide;
     for (;;) {
-        if (tid == 0) s_work = atomicAdd(&W.ctr[2 * list + 1], 1u);
+        if (tid == 0) s_work = take_work(W, list);
         __syncthreads();
         const uint32_t w = s_work;
         __syncthreads();
-        if (w >= *(volatile uint32_t *)&W.ctr[2 * list]) break;
+        if (w == 0xFFFFFFFFu) break;
         const uint2 wk = W.work[(size_t)list * W.work_stride + w];
         const uint32_t q = wk.x, p = wk.y;
         if (!GG_OK(q, W.q_cap, 12)) continue;
@@ -894,11 +906,11 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
 
     const int list = SMALL ? kListDenseSmall : kListDenseWide;
     for (;;) {
-        if (tid == 0) s_work = atomicAdd(&W.ctr[2 * list + 1], 1u);
+        if (tid == 0) s_work = take_work(W, list);
         __syncthreads();
         const uint32_t w = s_work;
         __syncthreads();
-        if (w >= *(volatile uint32_t *)&W.ctr[2 * list]) break;
+        if (w == 0xFFFFFFFFu) break;
         const uint2 wk = W.work[(size_t)list * W.work_stride + w];
         const uint32_t q = wk.x, p = wk.y;
         if (!GG_OK(q, W.q_cap, 12)) continue;
