@@ -36,11 +36,14 @@ namespace gg {
 constexpr uint32_t kBmThreads = 1024;
 constexpr uint32_t kBmChunks = 2048;      // 32-id chunks per query on this path
 // selection buffers of a query with >= k table entries, over the bitmap (which
-// nothing reads then): candidate keys, tie ids, tie keys, bucket counters
+// nothing reads then): candidate keys, tie ids, tie keys, bucket counters,
+// the ranked candidates
 constexpr uint32_t kBmScrTieIds = kCandCap * 8;
 constexpr uint32_t kBmScrTieKeys = kBmScrTieIds + kCandCap * 4;
 constexpr uint32_t kBmScrBuckets = kBmScrTieKeys + kCandCap / 2 * 8;
-constexpr uint32_t kBmScratch = kBmScrBuckets + 1024 * 4;
+constexpr uint32_t kBmScrRanked = kBmScrBuckets + 1024 * 4;
+constexpr uint32_t kBmRankMax = 256;      // entries above c* ordered by rank (more: a bitonic sort)
+constexpr uint32_t kBmScratch = kBmScrRanked + kBmRankMax * 8;
 static_assert(kBmChunks >= (uint32_t)kMaxK, "the chunk region holds the keys of a query with < k table entries");
 constexpr uint32_t kBmProbe = 128;        // longest probe run of the repeated-id table
 constexpr int kBmRound = 16;              // chunk loads in flight per lane
@@ -151,6 +154,7 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
     uint64_t *cand_s = (uint64_t *)(smem + L.bm);                         // [0, kCandCap)
     uint32_t *tie_ids = (uint32_t *)(smem + L.bm + kBmScrTieIds);         // [0, kCandCap)
     uint64_t *tie_keys = (uint64_t *)(smem + L.bm + kBmScrTieKeys);       // [0, kCandCap / 2)
+    uint64_t *ranked = (uint64_t *)(smem + L.bm + kBmScrRanked);          // [0, kBmRankMax)
     SelectScratch &ss = *(SelectScratch *)(smem + L.ss);
     uint32_t *hist = ss.hist;
     __shared__ uint32_t s_multi, s_ovf, s_n, s_big;
@@ -347,12 +351,20 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
                     if (at < (uint32_t)kCandCap) tie_ids[at] = e >> 8;
                 }
             }
-            if (warp == 0 && above <= 64) warp_sort_desc64(cand, above);
+            // the entries above c*: few and distinct, each placed at its rank
+            if (above <= kBmRankMax && tid < above) {
+                const uint64_t key = cand[tid];
+                uint32_t rank = 0;
+                for (uint32_t j = 0; j < above; ++j) rank += cand[j] > key ? 1u : 0u;
+                ranked[rank] = key;
+            }
             __syncthreads();
-            if (above > 64) {
+            if (above > kBmRankMax) {
                 const uint32_t hp2 = next_pow2(above);
                 for (uint32_t x = above + tid; x < hp2; x += kBmThreads) cand[x] = 0ull;
                 bitonic_sort_desc(cand, hp2);
+            } else {
+                cand = ranked;
             }
             const bool big = s_big != 0;
             if (big && next_pow2(n_eq) <= kCandCap / 2) {

@@ -337,17 +337,6 @@ __device__ __forceinline__ void bitonic_reg_stages(uint64_t &x0, uint64_t &x1, u
     x1 = desc ? lo : hi;
 }
 
-// Descending sort of n <= 64 keys by one whole warp, in registers (no block
-// barrier; the caller orders it against other warps).  Keys past n read as 0.
-__device__ __forceinline__ void warp_sort_desc64(uint64_t *a, uint32_t n) {
-    const uint32_t t = lane_id();
-    uint64_t x0 = 2 * t < n ? a[2 * t] : 0ull, x1 = 2 * t + 1 < n ? a[2 * t + 1] : 0ull;
-    for (uint32_t size = 2; size <= 64; size <<= 1) bitonic_reg_stages(x0, x1, t, size, size >> 1);
-    if (2 * t < n) a[2 * t] = x0;
-    if (2 * t + 1 < n) a[2 * t + 1] = x1;
-    __syncwarp();
-}
-
 // Descending bitonic sort of n (power of two) keys in shared memory.  Strides
 // up to 32 run in registers (shuffles); only the longer strides of the merges
 // of 128 keys and more go through shared memory, one barrier each.
