@@ -72,6 +72,8 @@ PROTOTYPES = {
     "genie_batch_stage": (ctypes.c_int, [P, P]),
     "genie_batch_launch": (ctypes.c_int, [P, P]),
     "genie_batch_fetch": (ctypes.c_int, [P, P, P, P]),
+    "genie_batch_submit": (ctypes.c_int, [P, P, I32]),
+    "genie_batch_collect": (ctypes.c_int, [P, P, P, P]),
     "genie_batch_autotune": (ctypes.c_int, [P, P, P]),
     "genie_batch_get_tuning": (ctypes.c_int, [P, P]),
     "genie_batch_set_tuning": (ctypes.c_int, [P, P]),

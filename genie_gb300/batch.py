@@ -55,6 +55,25 @@ class Batch:
                                        None if sc is None else sc.ctypes.data))
         return (ids[:n], cnt[:n], sc[:n]) if scores else (ids[:n], cnt[:n])
 
+    def submit(self, batch, scores=False):
+        """Asynchronous run: stage `batch`, enqueue its device work and result
+        download, and return; collect() waits and returns the results.  Two
+        batches used in turn overlap host staging with device work."""
+        from . import _check, lib
+        s = batch.struct()
+        _check(lib().genie_batch_submit(self._h, ctypes.byref(s), 1 if scores else 0))
+        self._staged = batch
+        self._submitted_scores = scores
+
+    def collect(self):
+        from . import _check, lib
+        scores = getattr(self, "_submitted_scores", False)
+        n = self._staged.total_k
+        ids, cnt, sc = self._outs(n, scores)
+        _check(lib().genie_batch_collect(self._h, ids.ctypes.data, cnt.ctypes.data,
+                                         None if sc is None else sc.ctypes.data))
+        return (ids[:n], cnt[:n], sc[:n]) if scores else (ids[:n], cnt[:n])
+
     def autotune(self, sample):
         from . import _check, lib
         t = _lib.GenieTuning()

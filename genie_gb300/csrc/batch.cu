@@ -25,11 +25,9 @@ struct genie_batch {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t stage_ev[kStages + 1] = {};
     // pinned staging
-    int64_t *h_item_off = nullptr, *h_out_off = nullptr;
-    int32_t *h_dim = nullptr, *h_low = nullptr, *h_up = nullptr;
-    float *h_weight = nullptr, *h_scores = nullptr;
+    int64_t *h_out_off = nullptr;
     uint8_t *h_weighted = nullptr;
-    uint32_t *h_k = nullptr, *h_dyn = nullptr, *h_ids = nullptr, *h_counts = nullptr, *h_err = nullptr;
+    uint32_t *h_k = nullptr, *h_dyn = nullptr, *h_err = nullptr;
     int32_t staged_q = 0;
     int64_t staged_sumk = 0;
     int last_kernels = 0;
@@ -45,8 +43,7 @@ genie_batch::~genie_batch() {
     for (cudaEvent_t e : stage_ev)
         if (e) cudaEventDestroy(e);
     if (stream) cudaStreamDestroy(stream);
-    void *pinned[] = {h_item_off, h_out_off, h_dim, h_low, h_up, h_weight, h_scores, h_weighted, h_k, h_dyn,
-                      h_ids, h_counts, h_err};
+    void *pinned[] = {h_out_off, h_weighted, h_k, h_dyn, h_err};
     for (void *p : pinned)
         if (p) cudaFreeHost(p);
     ws.release();
@@ -122,47 +119,46 @@ int stage_async(genie_batch *b, const genie_queries *q, cudaStream_t s) {
         const uint32_t k = q->k ? q->k[i] : q->uniform_k;
         if (k > b->cfg.max_k) return fail(GENIE_ERR_INVALID_ARG, "k=%u exceeds the batch capacity %u", k, b->cfg.max_k);
     }
-    memcpy(b->h_item_off, q->item_off, (Q + 1) * 8);
-    memcpy(b->h_dim, q->dim, n_items * 4);
-    memcpy(b->h_low, q->low, n_items * 4);
-    memcpy(b->h_up, q->up, n_items * 4);
-    if (q->weighted && q->weight) {
-        memcpy(b->h_weight, q->weight, n_items * 4);
-        memcpy(b->h_weighted, q->weighted, Q);
-    } else {
-        memset(b->h_weighted, 0, Q);
-    }
+    // The caller's item arrays are uploaded from where they are: a copy from
+    // pageable memory returns once the source may be reused, and on a
+    // coherently attached host it moves the bytes without a staging memcpy,
+    // which is faster than one through pinned buffers.  The arrays built here
+    // (k, result offsets, batch size) go through pinned staging.
+    // Exact-match items (up is the low array itself) travel once.
+    const bool exact = q->up == q->low;
+    const bool weighted = q->weighted && q->weight;
+    if (!weighted) memset(b->h_weighted, 0, Q);
     for (int64_t i = 0; i < Q; ++i) b->h_k[i] = q->k ? q->k[i] : q->uniform_k;
     memcpy(b->h_out_off, out_off.data(), (Q + 1) * 8);
     b->h_dyn[0] = (uint32_t)Q;
     b->h_dyn[1] = q->uniform_k;
+    b->h_dyn[2] = exact ? 1u : 0u;
     cudaError_t e = cudaSuccess;
     Workspace &ws = b->ws;
     auto h2d = [&](void *dst, const void *src, size_t n) {
         if (n && !e) e = cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, s);
     };
-    h2d(ws.item_off.p, b->h_item_off, (Q + 1) * 8);
-    h2d(ws.dim.p, b->h_dim, n_items * 4);
-    h2d(ws.low.p, b->h_low, n_items * 4);
-    h2d(ws.up.p, b->h_up, n_items * 4);
-    if (q->weighted && q->weight) h2d(ws.weight.p, b->h_weight, n_items * 4);
-    h2d(ws.weighted.p, b->h_weighted, Q);
+    h2d(ws.item_off.p, q->item_off, (Q + 1) * 8);
+    h2d(ws.dim.p, q->dim, n_items * 4);
+    h2d(ws.low.p, q->low, n_items * 4);
+    if (!exact) h2d(ws.up.p, q->up, n_items * 4);
+    if (weighted) h2d(ws.weight.p, q->weight, n_items * 4);
+    h2d(ws.weighted.p, weighted ? (const void *)q->weighted : (const void *)b->h_weighted, Q);
     h2d(ws.k.p, b->h_k, Q * 4);
     h2d(ws.out_off.p, b->h_out_off, (Q + 1) * 8);
-    h2d(b->dyn.p, b->h_dyn, 8);
+    h2d(b->dyn.p, b->h_dyn, 12);
     if (e) return cuda_fail(e, "batch upload");
     b->staged_q = (int32_t)Q;
     b->staged_sumk = out_off[Q];
     return GENIE_OK;
 }
 
+// The error word of the last launch into pinned memory (async on s); the
+// results themselves are downloaded by finish_fetch into the caller's buffers.
 int fetch_async(genie_batch *b, cudaStream_t s, bool scores) {
-    const int64_t n = b->staged_sumk;
+    (void)scores;
     const Work w = b->ws.view(b->cfg.max_queries, true);
     cudaError_t e = cudaMemcpyAsync(b->h_err, w.ctr + kCtrError, 4, cudaMemcpyDeviceToHost, s);
-    if (!e && n) e = cudaMemcpyAsync(b->h_ids, w.out_ids, n * 4, cudaMemcpyDeviceToHost, s);
-    if (!e && n) e = cudaMemcpyAsync(b->h_counts, w.out_counts, n * 4, cudaMemcpyDeviceToHost, s);
-    if (!e && n && scores) e = cudaMemcpyAsync(b->h_scores, w.out_scores, n * 4, cudaMemcpyDeviceToHost, s);
     return e ? cuda_fail(e, "batch download") : GENIE_OK;
 }
 
@@ -171,10 +167,14 @@ int finish_fetch(genie_batch *b, uint32_t *ids, uint32_t *counts, float *scores)
     if (e) return cuda_fail(e, "batch");
     int rc = check_device_error(*b->h_err);
     if (rc) return rc;
+    // results straight into the caller's buffers (faster than a download
+    // into pinned staging and a host copy out of it)
     const size_t n = (size_t)b->staged_sumk;
-    if (ids) memcpy(ids, b->h_ids, n * 4);
-    if (counts) memcpy(counts, b->h_counts, n * 4);
-    if (scores) memcpy(scores, b->h_scores, n * 4);
+    const Work w = b->ws.view(b->cfg.max_queries, true);
+    if (ids && n) e = cudaMemcpy(ids, w.out_ids, n * 4, cudaMemcpyDeviceToHost);
+    if (!e && counts && n) e = cudaMemcpy(counts, w.out_counts, n * 4, cudaMemcpyDeviceToHost);
+    if (!e && scores && n) e = cudaMemcpy(scores, w.out_scores, n * 4, cudaMemcpyDeviceToHost);
+    if (e) return cuda_fail(e, "batch download");
     return GENIE_OK;
 }
 
@@ -234,18 +234,10 @@ int genie_batch_create(genie_index *ix, const genie_batch_config *cfg, genie_bat
     if (!e) e = cudaEventCreate(&b->ev0);
     if (!e) e = cudaEventCreate(&b->ev1);
     for (int i = 0; i <= kStages && !e; ++i) e = cudaEventCreate(&b->stage_ev[i]);
-    if (!e) e = pin(b->h_item_off, Q + 1);
     if (!e) e = pin(b->h_out_off, Q + 1);
-    if (!e) e = pin(b->h_dim, I);
-    if (!e) e = pin(b->h_low, I);
-    if (!e) e = pin(b->h_up, I);
-    if (!e) e = pin(b->h_weight, I);
     if (!e) e = pin(b->h_weighted, Q);
     if (!e) e = pin(b->h_k, Q);
     if (!e) e = pin(b->h_dyn, 4);
-    if (!e) e = pin(b->h_ids, K);
-    if (!e) e = pin(b->h_counts, K);
-    if (!e) e = pin(b->h_scores, K);
     if (!e) e = pin(b->h_err, 4);
     if (e) {
         delete b;
@@ -434,4 +426,19 @@ int gg::batch_ready(genie_batch *b) {
 
 int gg::batch_collect(genie_batch *b, uint32_t *ids, uint32_t *counts, float *scores) {
     return finish_fetch(b, ids, counts, scores);
+}
+
+extern "C" int genie_batch_submit(genie_batch *b, const genie_queries *q, int32_t want_scores) {
+    if (!b || !q) return fail(GENIE_ERR_INVALID_ARG, "NULL argument");
+    cudaSetDevice(b->ix->device);
+    cudaError_t e = cudaStreamSynchronize(b->stream);     // the staging buffers are free again
+    if (e) return cuda_fail(e, "batch");
+    b->staged_sumk = 0;
+    return batch_submit_async(b, q, want_scores != 0);
+}
+
+extern "C" int genie_batch_collect(genie_batch *b, uint32_t *out_ids, uint32_t *out_counts, float *out_scores) {
+    if (!b) return fail(GENIE_ERR_INVALID_ARG, "batch is NULL");
+    cudaSetDevice(b->ix->device);
+    return batch_collect(b, out_ids, out_counts, out_scores);
 }

@@ -66,7 +66,8 @@ struct DevQueries {
     uint32_t uniform_k;
     const int64_t *out_off;
     // optional device-side size of a captured batch: dyn[0] = queries in this
-    // run (<= n_queries, the capacity), dyn[1] = uniform k
+    // run (<= n_queries, the capacity), dyn[1] = uniform k, dyn[2] = 1 when
+    // every item is exact (up = low; the up array is not sent)
     const uint32_t *dyn;
 };
 

@@ -65,6 +65,7 @@ __global__ void __launch_bounds__(kPlanThreads, 4) k_plan(DevIndex ix, DevQuerie
     const int32_t m = (int32_t)(i1 - i0);
     const uint32_t k = Q.k ? Q.k[q] : (Q.dyn ? Q.dyn[1] : Q.uniform_k);
     const bool weighted = Q.weighted && Q.weight && Q.weighted[q];
+    const bool exact = Q.dyn && Q.dyn[2];      // a batch of exact items sends no upper bounds
     if (tid == 0) {
         s_total = 0;
         s_units = 0;
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(kPlanThreads, 4) k_plan(DevIndex ix, DevQuerie
     uint32_t nk_first = 0, inc_first = 1;
     for (int64_t i = i0 + tid; i < i1; i += nt) {
         if (!GG_OK(i, W.items_cap, 7)) break;
-        int32_t d = Q.dim[i], lo = Q.low[i], hi = Q.up[i];
+        int32_t d = Q.dim[i], lo = Q.low[i], hi = exact ? lo : Q.up[i];
         int64_t k0 = 0, nk = 0, a = 0, e = 0;
         if (d >= 0 && d < ix.n_dims) {
             int32_t mn = ix.dim_min[d], mx = ix.dim_max[d];

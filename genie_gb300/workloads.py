@@ -43,6 +43,14 @@ def config0(n=1000, d=128, q=100, k=10, seed=1234):
 def config1(n=1_000_000, d=240, q=1024, k=100, buckets=8192, seed=1235):
     rng = np.random.default_rng(seed)
     values = rng.integers(0, buckets, size=(n, d), dtype=np.int32)
+    return values, config1_queries(values, q, k, buckets, rng=rng)
+
+
+def config1_queries(values, q=1024, k=100, buckets=8192, seed=None, rng=None):
+    """A config1 query batch over given values: half the queries derived from
+    stored objects with 60% of their items redrawn, half uniform."""
+    rng = rng if rng is not None else np.random.default_rng(seed)
+    n, d = values.shape
     qv = rng.integers(0, buckets, size=(q, d), dtype=np.int32)
     derived = np.arange(q) < q // 2
     src = rng.integers(0, n, q)
@@ -50,7 +58,7 @@ def config1(n=1_000_000, d=240, q=1024, k=100, buckets=8192, seed=1235):
     qv[derived] = np.where(keep[derived], values[src[derived]], qv[derived])
     dims = np.tile(np.arange(d, dtype=np.int32), q)
     flat = qv.ravel()
-    return values, _batch(np.arange(q + 1) * d, dims, flat, flat, np.full(q, k))
+    return _batch(np.arange(q + 1) * d, dims, flat, flat, np.full(q, k))
 
 
 def zipf_ranks(rng, size, s=1.1, n_terms=65536):

@@ -229,6 +229,15 @@ int genie_batch_stage(genie_batch *b, const genie_queries *q);
 int genie_batch_launch(genie_batch *b, void *stream);
 /* Wait for the last launch and copy its results to host buffers. */
 int genie_batch_fetch(genie_batch *b, uint32_t *out_ids, uint32_t *out_counts, float *out_scores);
+/* Asynchronous genie_batch_run in two calls.  submit waits for the batch's
+ * previous work (its pinned staging is reused), validates and copies the
+ * queries into that staging, enqueues the upload, the device work and the
+ * result download on the batch's stream, and returns.  collect waits for it
+ * and copies the results out (out_scores only if submitted with want_scores).
+ * Two batches used in turn overlap one batch's host-side staging with the
+ * other's device work. */
+int genie_batch_submit(genie_batch *b, const genie_queries *q, int32_t want_scores);
+int genie_batch_collect(genie_batch *b, uint32_t *out_ids, uint32_t *out_counts, float *out_scores);
 /* Time candidate tunings on a sample batch on the device; keeps the fastest. */
 int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuning *chosen);
 int genie_batch_get_tuning(const genie_batch *b, genie_tuning *out);

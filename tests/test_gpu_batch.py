@@ -158,3 +158,29 @@ def test_batch_capacity_errors(genie):
         bt.run(genie.QueryBatch([0, 1], [0], [0], [0], 6))
     ids, cnt = bt.run(genie.QueryBatch([0, 1], [0], [0], [0], 5))
     assert list(cnt) == [1] * 5
+
+
+def test_batch_submit_collect_in_turn(genie, oracle):
+    """Two batches used in turn through submit / collect (the pipelined
+    public path) give every query batch the oracle's results."""
+    from genie_gb300 import workloads
+    values, first = workloads.config1(n=20_000, d=24, q=48, k=10, buckets=64)
+    t = genie.Table.from_values(values)
+    ox = oracle.Index(values)
+    batches = [first] + [workloads.config1_queries(values, 48, 10, buckets=64, seed=s) for s in (11, 12, 13)]
+    pair = (genie.Batch(t, 48, 48 * 24, 10), genie.Batch(t, 48, 48 * 24, 10))
+    expect = [ox.search(_qb(genie, b).as_oracle_batch())[:2] for b in batches]
+    pend, got = [], []
+    order = list(range(len(batches))) * 2
+    for i, j in enumerate(order):
+        b = pair[i % 2]
+        if len(pend) == 2:
+            bb, jj = pend.pop(0)
+            got.append((jj, bb.collect()))
+        b.submit(_qb(genie, batches[j]))
+        pend.append((b, j))
+    for bb, jj in pend:
+        got.append((jj, bb.collect()))
+    assert len(got) == len(order)
+    for j, (ids, cnt) in got:
+        assert np.array_equal(ids, expect[j][0]) and np.array_equal(cnt, expect[j][1])
