@@ -166,10 +166,12 @@ int validate_queries(const genie_queries *q, std::vector<int64_t> &out_off, int6
     return GENIE_OK;
 }
 
-// Exact number of (dim,value) lists the batch's items cover (one unit each).
+// Number of (dim,value) lists the batch's items cover (one unit each): exact,
+// or for exact-match items (up is the low array) the item count, a bound.
 int64_t count_units(const HostIndex &h, const genie_queries *q) {
     int64_t units = 0;
     const int64_t n = q->n_queries > 0 ? q->item_off[q->n_queries] : 0;
+    if (q->up == q->low) return n;      // exact items: at most one list each (a bound the plan stays within)
     for (int64_t i = 0; i < n; ++i) {
         const int32_t d = q->dim[i];
         if (d < 0 || d >= h.n_dims) continue;
