@@ -191,7 +191,7 @@ int check_device_error(uint32_t err) {
     if (err & kErrWeight) return fail(GENIE_ERR_INVALID_ARG, "a weighted query holds a weight that is not finite and > 0");
     if (err & kErrCapacity) return fail(GENIE_ERR_INVALID_ARG, "k outside [1, %d]", kMaxK);
     if (err & kErrTimeout)
-        return fail(GENIE_ERR_DEVICE_TIMEOUT, "a device wait of the bitmap kernel ran out of time");
+        return fail(GENIE_ERR_DEVICE_TIMEOUT, "a bounded device wait ran out of time");
     if (err & kErrUnits)
         return fail(GENIE_ERR_INVALID_ARG, "the batch's items cover more (dim,value) lists than its unit capacity");
     if (err) return fail(GENIE_ERR_CUDA, "device reported error flags 0x%x", err);

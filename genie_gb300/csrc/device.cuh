@@ -298,19 +298,12 @@ __device__ __forceinline__ uint64_t make_key(uint32_t prim, uint32_t id) {
 __device__ __forceinline__ uint32_t key_prim(uint64_t k) { return (uint32_t)(k >> 32); }
 __device__ __forceinline__ uint32_t key_id(uint64_t k) { return 0xFFFFFFFFu - (uint32_t)k; }
 
-// A group of threads that cooperates like a block: the whole block, or the
-// warps [1, 1 + N/32) of a warp-specialized block, synchronized by named
-// barrier 1 (the first warp runs on its own).
+// A group of threads that cooperates like a block (rank, size, barrier); the
+// helpers below take one, here always the whole block.
 struct BlockGroup {
     __device__ static uint32_t rank() { return threadIdx.x; }
     __device__ static uint32_t size() { return blockDim.x; }
     __device__ static void sync() { __syncthreads(); }
-};
-template <uint32_t N>
-struct TailGroup {
-    __device__ static uint32_t rank() { return threadIdx.x - 32u; }
-    __device__ static uint32_t size() { return N; }
-    __device__ static void sync() { asm volatile("bar.sync 1, %0;" ::"n"(N) : "memory"); }
 };
 
 // Compare-exchange: the larger key when keep_max, else the smaller.
