@@ -215,7 +215,8 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
         // ---- stage: chunk entries of every list
         const uint32_t nch = (uint32_t)((sp_len + 31) / 32);
         uint32_t n_chunks = 0;
-        const uint32_t c0 = block_excl_scan(nch, ss.tmp, &n_chunks);     // ends with a barrier
+        // (the previous query ended with a barrier; the stream starts after one)
+        const uint32_t c0 = block_excl_scan_lean(nch, ss.tmp, &n_chunks);
         for (uint32_t c = 0; c < nch && c0 + c < kBmChunks; ++c)
             chunk[c0 + c] = make_uint2((uint32_t)(sp_start + 32 * (int64_t)c),
                                        (uint32_t)min((int64_t)32, sp_len - 32 * (int64_t)c));
@@ -340,7 +341,7 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
             const uint32_t bc = tid < nb ? bcnt[tid] : 0u;
             if (bc > 32) s_big = 1;      // a crowded id range: sort all ties instead
             uint32_t tot = 0;
-            const uint32_t boff = block_excl_scan(bc, ss.tmp, &tot);     // ends with a barrier
+            const uint32_t boff = block_excl_scan_lean(bc, ss.tmp, &tot);     // barriers before and after
             if (tid < nb) bcnt[tid] = boff;                              // cursor
             __syncthreads();
             for (uint32_t b = 0; b < n_multi; b += kBmThreads) {

@@ -281,6 +281,25 @@ __device__ uint32_t group_excl_scan(uint32_t v, uint32_t *tmp, uint32_t *total) 
     return tmp[w] + incl - v;
 }
 
+// block_excl_scan without its first and last barriers, for callers that
+// order the earlier readers of s_tmp before the call and its later writers
+// after it (a barrier on each side within the caller's own flow).
+__device__ __forceinline__ uint32_t block_excl_scan_lean(uint32_t v, uint32_t *s_tmp, uint32_t *total) {
+    const uint32_t nw = (blockDim.x + 31) >> 5;
+    const uint32_t incl = warp_incl_scan(v);
+    if (lane_id() == 31) s_tmp[warp_id()] = incl;
+    __syncthreads();
+    if (warp_id() == 0) {
+        const uint32_t x = lane_id() < nw ? s_tmp[lane_id()] : 0u;
+        const uint32_t xi = warp_incl_scan(x);
+        if (lane_id() < nw) s_tmp[lane_id()] = xi - x;
+        if (lane_id() == nw - 1) s_tmp[32] = xi;
+    }
+    __syncthreads();
+    if (total) *total = s_tmp[32];
+    return s_tmp[warp_id()] + incl - v;
+}
+
 // Warp-aggregated shared-memory histogram increment: lanes holding the same
 // bin combine into one atomic (__match_any_sync).  All 32 lanes must call.
 __device__ __forceinline__ void hist_add(uint32_t *hist, uint32_t bin, bool active) {
