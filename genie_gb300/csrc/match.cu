@@ -53,7 +53,7 @@ __device__ __forceinline__ int64_t dense_parts(int64_t total, int64_t ntiles, in
     return pd < 1 ? 1 : pd;
 }
 
-__global__ void __launch_bounds__(kPlanThreads, 4) k_plan(DevIndex ix, DevQueries Q, Work W, Tuning T) {
+__global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQueries Q, Work W, Tuning T) {
     __shared__ unsigned long long s_total, s_units, s_unit0;
     __shared__ unsigned int s_maxw, s_bad;
     __shared__ uint32_t s_tmp[48];
