@@ -166,12 +166,15 @@ int validate_queries(const genie_queries *q, std::vector<int64_t> &out_off, int6
     return GENIE_OK;
 }
 
-// Number of (dim,value) lists the batch's items cover (one unit each): exact,
-// or for exact-match items (up is the low array) the item count, a bound.
+// Units a batch may need: a query whose items each cover at most one
+// (dim,value) list uses its items as units; any other takes one unit per
+// covered list past the batch's items.  So the item count, plus for a batch
+// with range items the lists they cover (a bound).  Exact-match items (up is
+// the low array) cover one list at most.
 int64_t count_units(const HostIndex &h, const genie_queries *q) {
     int64_t units = 0;
     const int64_t n = q->n_queries > 0 ? q->item_off[q->n_queries] : 0;
-    if (q->up == q->low) return n;      // exact items: at most one list each (a bound the plan stays within)
+    if (q->up == q->low) return n;
     for (int64_t i = 0; i < n; ++i) {
         const int32_t d = q->dim[i];
         if (d < 0 || d >= h.n_dims) continue;
@@ -179,7 +182,7 @@ int64_t count_units(const HostIndex &h, const genie_queries *q) {
         const int64_t hi = std::min<int64_t>(q->up[i], h.dim_max[d]);
         if (hi >= lo) units += hi - lo + 1;
     }
-    return units;
+    return n + units;
 }
 
 int check_device_error(uint32_t err) {

@@ -30,10 +30,12 @@ void read_oob(unsigned long long out[4]) {
 // Query compile on the device, one CTA per query in one launch: clamp every
 // item (Query::attr / Query::build, query/query.cc:87-113, 273-333), count the
 // (dim,value) lists it covers and the posting ids it touches, the fixed-point
-// scale of a weighted query; take a contiguous range of units from a device
-// counter (ranges of different queries need no order between them); write one
-// unit per covered list (a sorted posting list, or the segment range of a
-// compressed one); then the bitmap/sparse/dense decision and the work lists.
+// scale of a weighted query; the query's units (one per covered list: a
+// sorted posting list, or the segment range of a compressed one) are its items
+// when each covers at most one list, else a contiguous range taken from a
+// device counter past the batch's items (ranges of different queries need no
+// order between them); then the bitmap/sparse/dense decision and the work
+// lists.
 // A range item covers several lists whose concatenation is not sorted, so
 // every later search inside a span happens per unit.
 
@@ -55,7 +57,7 @@ __device__ __forceinline__ int64_t dense_parts(int64_t total, int64_t ntiles, in
 
 __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQueries Q, Work W, Tuning T) {
     __shared__ unsigned long long s_total, s_units, s_unit0;
-    __shared__ unsigned int s_maxw, s_bad;
+    __shared__ unsigned int s_maxw, s_bad, s_multi;
     __shared__ uint32_t s_tmp[48];
     const int64_t q = blockIdx.x;
     const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
@@ -71,6 +73,7 @@ __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQuerie
         s_units = 0;
         s_maxw = 0;
         s_bad = 0;
+        s_multi = 0;
     }
     __syncthreads();
     int32_t scale = 0;
@@ -115,6 +118,20 @@ __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQuerie
         }
         uint32_t inc = 1;
         if (weighted) inc = (uint32_t)__double2ll_rn(ldexp((double)Q.weight[i], scale));
+        // An item covering at most one list is also unit i: when every item
+        // of the query is, the query's units are its items and nothing more
+        // is written.  Otherwise the query takes a unit range past the
+        // batch's items and these slots, in its own item range, stay unread.
+        if (nk <= 1 && i < W.units_cap) {
+            if (ix.codec) {
+                a = nk ? ix.key_seg[k0] : 0;
+                e = nk ? ix.key_seg[k0 + 1] : 0;
+            }
+            W.span_start[i] = a;
+            W.span_len[i] = e - a;
+            W.inc[i] = inc;
+        }
+        if (nk > 1) s_multi = 1;
         if (i == i0 + tid) {
             k0_first = k0;
             nk_first = (uint32_t)nk;
@@ -135,14 +152,18 @@ __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQuerie
         atomicAdd(&s_units, (unsigned long long)units);
     }
     __syncthreads();
-    if (tid == 0) s_unit0 = atomicAdd((unsigned long long *)&W.ctr[kCtrUnits], s_units);
+    const bool single = s_multi == 0;      // block-uniform
+    if (tid == 0)
+        s_unit0 = single ? (unsigned long long)i0
+                         : (unsigned long long)Q.item_off[nq] +
+                               atomicAdd((unsigned long long *)&W.ctr[kCtrUnits], s_units);
     __syncthreads();
-    const int64_t unit0 = (int64_t)s_unit0, n_units = (int64_t)s_units;
+    const int64_t unit0 = (int64_t)s_unit0, n_units = single ? (int64_t)m : (int64_t)s_units;
     total = s_total;
     const bool fits = unit0 + n_units <= W.units_cap;
     if (tid == 0 && !fits) atomicOr(&W.ctr[kCtrError], kErrUnits);
-    // one unit per covered list
-    if (fits) {
+    // one unit per covered list (a query with several lists in one item)
+    if (fits && !single) {
         int64_t base = unit0;
         for (int64_t c = i0; c < i1; c += nt) {
             const int64_t i = c + tid;

@@ -25,7 +25,7 @@ namespace {
 // Largest batch one call accepts.
 constexpr int64_t kNaMaxQueries = 1024;
 constexpr int64_t kNaMaxItems = 262144;
-constexpr int64_t kNaMaxUnits = 262144;     // (dim,value) lists the items cover
+constexpr int64_t kNaMaxUnits = 262144;     // the items, plus lists of queries with multi-list items
 constexpr int64_t kNaMaxResults = 32768;    // sum of k over the batch
 
 constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }

@@ -179,8 +179,9 @@ int genie_search_multi(genie_index *const *ix, const genie_queries *q, int32_t n
  * are DEVICE pointers (q->n_queries and q->uniform_k are host values);
  * n_items = item_off[n_queries], total_k = sum of k.  The workspace is a
  * fixed 16 MiB device array inside the library, shared by every call: at
- * most 1024 queries, 262144 items, 262144 covered (dim,value) lists and
- * 32768 results per call, larger batches are rejected with
+ * most 1024 queries, 262144 items, 262144 list units (the items, plus the
+ * (dim,value) lists covered by queries whose items cover several lists
+ * each) and 32768 results per call, larger batches are rejected with
  * GENIE_ERR_INVALID_ARG.  The first call on a device looks up the array's
  * address (and prepares the kernels); make it before any stream capture.
  * Calls are serialised and wait for their device work on `stream` (a
@@ -197,7 +198,8 @@ typedef struct {
     int64_t max_items;
     uint32_t max_k;
     int32_t use_graph;       /* capture the device work as one CUDA graph */
-    int64_t max_units;       /* (dim,value) lists the items may cover; 0: 16 * max_items */
+    int64_t max_units;       /* list units: the items, plus the (dim,value) lists covered by queries
+                                whose items cover several lists each; 0: 16 * max_items */
 } genie_batch_config;
 
 /* Kernel shape knobs picked by the autotuner (0 keeps the current value). */
