@@ -11,8 +11,11 @@ to exact top-k.  Prints one JSON line:
   value      queries/s with the batch resident in HBM: the captured CUDA graph
              (device-side query compile + persistent match kernels + top-k),
              CUDA events on the launching stream, L2 flushed before every step
-  e2e        queries/s through genie_batch_run from host buffers: pinned H2D of
-             the queries, the graph, D2H of ids/counts, per step
+  e2e        queries/s through the public batch API from host buffers: every
+             step uploads its queries and downloads its ids/counts; two
+             batches in turn (genie_batch_submit / genie_batch_collect) over
+             four query batches of the workload; e2e.sequential_value is one
+             genie_batch_run per step
   roofline   posting-list bytes touched per launch / the dominant kernel's
              event-timed duration, against the measured HBM copy bandwidth
   cpu_baseline  the CPU oracle on this host's cores over the same batch
