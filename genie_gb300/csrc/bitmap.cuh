@@ -47,6 +47,7 @@ constexpr uint32_t kBmScratch = kBmScrRanked + kBmRankMax * 8;
 static_assert(kBmChunks >= (uint32_t)kMaxK, "the chunk region holds the keys of a query with < k table entries");
 constexpr uint32_t kBmProbe = 128;        // longest probe run of the repeated-id table
 constexpr int kBmRound = 16;              // chunk loads in flight per lane
+static_assert(kBmRound == 16, "the repeat loop selects v[r] by four bits of r");
 constexpr uint32_t kBmDescRing = 128;     // query descriptors kept in shared memory
 constexpr uint32_t kBmDescFill = 64;      // descriptors loaded at a time
 
@@ -293,10 +294,15 @@ __global__ void __launch_bounds__(kBmThreads, 1) k_bitmap(DevIndex ix, DevQuerie
                 if (rep) {
                     const uint32_t r = __ffs(rep) - 1;
                     rep &= rep - 1;
-                    uint32_t id = v[0];
+                    // v[r] by a tree of selects on the bits of r (kBmRound = 16)
+                    uint32_t t8[8], t4[4], t2[2];
 #pragma unroll
-                    for (int j = 1; j < kBmRound; ++j) id = (r == (uint32_t)j) ? v[j] : id;
-                    repeat(id);
+                    for (int j = 0; j < 8; ++j) t8[j] = (r & 1u) ? v[2 * j + 1] : v[2 * j];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) t4[j] = (r & 2u) ? t8[2 * j + 1] : t8[2 * j];
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) t2[j] = (r & 4u) ? t4[2 * j + 1] : t4[2 * j];
+                    repeat((r & 8u) ? t2[1] : t2[0]);
                 }
             }
         }
