@@ -16,11 +16,12 @@
 //           first occurrence sets the id's bit, a repeat goes to the table
 //           (id<<8 | count, count >= 2), which also keeps a histogram of its
 //           counts;
-//   select  with >= k table ids, the histogram gives the k-th count c*; one
-//           warp sorts the (few) ids above c*, and the ids at c* go through a
-//           counting sort by id range (1024 buckets, each then sorted in
-//           place; a crowded bucket falls back to a bitonic sort of all ties);
-//           the result is the first k.  With fewer, the result is the whole
+//   select  with >= k table ids, the histogram gives the k-th count c*; the
+//           (few) ids above c* are placed by rank, and the ids at c* go
+//           through a counting sort by id range (1024 buckets, each then
+//           sorted in place; a crowded bucket falls back to a bitonic sort of
+//           all ties); these buffers lie over the bitmap, which nothing reads
+//           any more; the result is the first k.  With fewer, the result is the whole
 //           table, then the smallest ids whose bit is set and that are not in
 //           the table (count 1).  A full table hands the query to the dense
 //           kernel.  New table entries are listed as they are made, so these
