@@ -43,7 +43,8 @@ class GenieServerConfig(ctypes.Structure):
 class GenieServerReport(ctypes.Structure):
     _fields_ = [("submitted", I64), ("completed", I64), ("rejected", I64), ("batches", I64),
                 ("mean_batch", ctypes.c_double), ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double),
-                ("max_us", ctypes.c_double), ("throughput_qps", ctypes.c_double)]
+                ("max_us", ctypes.c_double), ("throughput_qps", ctypes.c_double), ("held", I64),
+                ("peak_in_flight_bytes", I64)]
 
 
 # name -> (restype, argtypes); mirrors include/genie_gb300.h

@@ -195,6 +195,9 @@ int check_device_error(uint32_t err) {
     if (err & kErrCapacity) return fail(GENIE_ERR_INVALID_ARG, "k outside [1, %d]", kMaxK);
     if (err & kErrTimeout)
         return fail(GENIE_ERR_DEVICE_TIMEOUT, "a bounded device wait ran out of time");
+    if (err & kErrBounds)
+        return fail(GENIE_ERR_INVALID_ARG, "a query's items or result slots lie outside the batch's arrays "
+                                           "(item_off or out_off and k disagree with the sizes passed)");
     if (err & kErrUnits)
         return fail(GENIE_ERR_INVALID_ARG, "the batch's items cover more (dim,value) lists than its unit capacity");
     if (err) return fail(GENIE_ERR_CUDA, "device reported error flags 0x%x", err);

@@ -31,7 +31,8 @@ constexpr uint32_t kBmMaxIds = 40 * 1024;
 // last position stay inside the allocation
 constexpr size_t kIdsPadBytes = 128;
 
-enum : uint32_t { kErrWeight = 1, kErrOverflow = 2, kErrCapacity = 4, kErrUnits = 8, kErrTimeout = 16 };
+enum : uint32_t { kErrWeight = 1, kErrOverflow = 2, kErrCapacity = 4, kErrUnits = 8, kErrTimeout = 16,
+                  kErrBounds = 32 };
 
 struct DevIndex {
     const uint32_t *ids;
@@ -129,7 +130,9 @@ struct Work {
     uint32_t *out_ids;
     uint32_t *out_counts;
     float *out_scores;     // may be null
-    // capacities (units_cap is enforced; the others bound the checked build)
+    // capacities: units_cap, items_cap and out_cap are enforced by the plan
+    // kernel in every build (a query outside them gets no work); q_cap
+    // bounds the checked build
     int64_t units_cap;
     int64_t items_cap;
     int64_t q_cap;

@@ -57,7 +57,7 @@ __device__ __forceinline__ int64_t dense_parts(int64_t total, int64_t ntiles, in
 
 __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQueries Q, Work W, Tuning T) {
     __shared__ unsigned long long s_total, s_units, s_unit0;
-    __shared__ unsigned int s_maxw, s_bad, s_multi;
+    __shared__ unsigned int s_maxw, s_bad, s_multi, s_oob;
     __shared__ uint32_t s_tmp[48];
     const int64_t q = blockIdx.x;
     const int64_t nq = Q.dyn ? (int64_t)Q.dyn[0] : (int64_t)Q.n_queries;
@@ -66,6 +66,25 @@ __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQuerie
     const int64_t i0 = Q.item_off[q], i1 = Q.item_off[q + 1];
     const int32_t m = (int32_t)(i1 - i0);
     const uint32_t k = Q.k ? Q.k[q] : (Q.dyn ? Q.dyn[1] : Q.uniform_k);
+    // The query's items and result slots must lie inside the workspace, also
+    // when the caller's device arrays (item_off, out_off, k) disagree with the
+    // sizes it passed: a query outside them is reported and gets no work, so
+    // nothing downstream indexes past the item, unit, scratch or result arrays.
+    if (tid == 0) {
+        const int64_t last = Q.item_off[nq], o = Q.out_off[q];
+        s_oob = !(i0 >= 0 && i0 <= i1 && i1 <= last && last <= W.items_cap && o >= 0 && o <= W.out_cap &&
+                  (int64_t)k <= W.out_cap - o);
+        if (s_oob) {
+            atomicOr(&W.ctr[kCtrError], kErrBounds);
+            QInfo none{};
+            none.cls = kClsNone;
+            W.qinfo[q] = none;
+            W.done[q] = 0;
+            W.qstate[q] = 0;
+        }
+    }
+    __syncthreads();
+    if (s_oob) return;
     const bool weighted = Q.weighted && Q.weight && Q.weighted[q];
     const bool exact = Q.dyn && Q.dyn[2];      // a batch of exact items sends no upper bounds
     if (tid == 0) {

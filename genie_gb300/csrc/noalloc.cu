@@ -123,7 +123,10 @@ extern "C" int genie_search_noalloc(genie_index *ix, const genie_queries *q, con
     w.out_counts = out_counts;
     w.out_scores = out_scores;
     w.units_cap = kNaMaxUnits;
-    w.items_cap = kNaMaxItems;
+    // the plan kernel holds every query to these (item_off[n_queries] <=
+    // n_items, out_off[q] + k[q] <= total_k) before anything is written, so a
+    // device array that disagrees with the host sizes is an error, not a fault
+    w.items_cap = n_items;
     w.q_cap = kNaMaxQueries;
     w.out_cap = total_k;
     DevQueries dq;

@@ -42,6 +42,7 @@ struct Request {
     int status = GENIE_OK;
     std::string error;
     bool done = false;
+    bool held = false;                 // its launch waited for in-flight memory to free up
 };
 
 // Device-side state a request holds while in flight: its items and plan rows,
@@ -77,6 +78,7 @@ struct genie_server {
     bool running = false, stop = false;
     int64_t in_flight_bytes = 0;
     // statistics since the last reset
+    int64_t held = 0, peak_in_flight_bytes = 0;
     std::vector<int64_t> lat_ns;
     int64_t submitted = 0, completed = 0, rejected = 0, batches = 0, batched = 0;
     int64_t first_arrival = INT64_MAX, last_done = 0;
@@ -181,7 +183,13 @@ void genie_server::loop() {
                 for (Request *q : sv.pending) {
                     if (q->arrival_ns > now || (int64_t)ready >= cfg.max_queries) break;
                     if (items + (int64_t)q->dim.size() > cfg.max_items) break;
-                    if (cfg.memory_budget > 0 && in_flight_bytes + bytes + q->bytes > cfg.memory_budget) break;
+                    if (cfg.memory_budget > 0 && in_flight_bytes + bytes + q->bytes > cfg.memory_budget) {
+                        if (!q->held) {          // admission holds it back until memory frees up
+                            q->held = true;
+                            ++held;
+                        }
+                        break;
+                    }
                     ++ready;
                     items += (int64_t)q->dim.size();
                     bytes += q->bytes;
@@ -229,6 +237,7 @@ void genie_server::loop() {
                 const int rc = batch_submit_async(sl.b, &gq, true);
                 sl.bytes = bytes;
                 in_flight_bytes += bytes;
+                peak_in_flight_bytes = std::max(peak_in_flight_bytes, in_flight_bytes);
                 sl.busy = true;
                 ++batches;
                 batched += (int64_t)ready;
@@ -426,6 +435,8 @@ int genie_server_stats(genie_server *s, genie_server_report *out) {
         out->rejected = s->rejected;
         out->batches = s->batches;
         out->mean_batch = s->batches ? (double)s->batched / (double)s->batches : 0.0;
+        out->held = s->held;
+        out->peak_in_flight_bytes = s->peak_in_flight_bytes;
         const int64_t span = s->last_done - s->first_arrival;
         out->throughput_qps = (s->completed && span > 0) ? (double)s->completed * 1e9 / (double)span : 0.0;
     }
@@ -446,6 +457,8 @@ int genie_server_reset_stats(genie_server *s) {
     std::lock_guard<std::mutex> lk(s->m);
     s->lat_ns.clear();
     s->submitted = s->completed = s->rejected = s->batches = s->batched = 0;
+    s->held = 0;
+    s->peak_in_flight_bytes = s->in_flight_bytes;
     s->first_arrival = INT64_MAX;
     s->last_done = 0;
     return GENIE_OK;

@@ -281,6 +281,8 @@ typedef struct {
     double mean_batch;        /* requests per batch */
     double p50_us, p99_us, max_us;   /* arrival -> result ready, completed requests since the last reset */
     double throughput_qps;    /* completed / (last completion - first arrival) */
+    int64_t held;             /* requests whose launch waited for in-flight memory under memory_budget */
+    int64_t peak_in_flight_bytes;  /* most request state on the device at once (the budget's measure) */
 } genie_server_report;
 
 int genie_server_create(const genie_server_config *cfg, genie_server **out);

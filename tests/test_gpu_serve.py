@@ -79,3 +79,29 @@ def test_admission_limits(genie):
     st = srv.stats()
     assert st["rejected"] == 1 and st["completed"] == 2 and st["batches"] == 2
     srv.close()
+
+
+def test_memory_budget_holds_requests_back(genie):
+    """A budget that fits about two requests' device state: admission holds
+    the rest until memory frees up, the in-flight peak never passes the
+    budget, and every answer equals the same query searched alone."""
+    from genie_gb300 import workloads
+    v3, b3 = workloads.config3(n=120_000, q=24)
+    t3 = genie.Table.from_values(v3)
+    budget = 45_000
+    srv = genie.Server(max_queries=16, max_items=16 * 128, max_k=100, slots_per_index=2, window_us=0,
+                       memory_budget=budget)
+    a = srv.add_index(t3)
+    srv.start()
+    first = srv.submit(a, _qb(genie, b3))          # all 24 arrive at once
+    for q in range(24):
+        k = int(b3["k"][q])
+        ids, cnt, sc, _ = srv.wait(first + q, k)
+        sid, scnt, ssc = genie.search(t3, _qb(genie, _slice(b3, q, q + 1)), scores=True)
+        assert np.array_equal(ids, sid) and np.array_equal(cnt, scnt) and np.array_equal(sc, ssc), q
+    st = srv.stats()
+    assert st["completed"] == 24
+    assert st["held"] > 0
+    assert 0 < st["peak_in_flight_bytes"] <= budget
+    assert st["batches"] >= 12                    # never more than two requests on the device at once
+    srv.close()
