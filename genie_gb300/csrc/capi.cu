@@ -85,8 +85,9 @@ cudaError_t Workspace::reserve(int64_t Q, int64_t items, int64_t units, int64_t 
     RES(ctr, kCtrWords * 4);
     RES(qstate, Q * 4 + 16);
     RES(done, Q * 4 + 16);
-    RES(part_cnt, Q * kMaxParts * 4 + 16);
-    RES(scratch, sumk * kMaxParts * 8 + 16);
+    RES(lb, Q * 4 + 16);
+    RES(part_cnt, Q * kMaxDenseParts * 4 + 16);
+    RES(scratch, sumk * kMaxDenseParts * 8 + 16);
     RES(out_ids, sumk * 4 + 16);
     RES(out_counts, sumk * 4 + 16);
     RES(out_scores, sumk * 4 + 16);
@@ -102,7 +103,7 @@ cudaError_t Workspace::reserve(int64_t Q, int64_t items, int64_t units, int64_t 
 void Workspace::release() {
     DevBuf *all[] = {&item_off, &dim, &low, &up, &weight, &weighted, &k, &out_off, &item_k0, &item_nk,
                      &item_inc, &span_start,
-                     &span_len, &inc, &qinfo, &work, &ctr, &qstate, &done, &part_cnt, &scratch,
+                     &span_len, &inc, &qinfo, &work, &ctr, &qstate, &done, &lb, &part_cnt, &scratch,
                      &out_ids, &out_counts, &out_scores};
     for (DevBuf *b : all) b->release();
 }
@@ -121,8 +122,10 @@ Work Workspace::view(int64_t Q, bool scores) const {
     w.ctr = (uint32_t *)ctr.p;
     w.qstate = (uint32_t *)qstate.p;
     w.done = (uint32_t *)done.p;
+    w.lb = (uint32_t *)lb.p;
     w.part_cnt = (uint32_t *)part_cnt.p;
     w.scratch = (uint64_t *)scratch.p;
+    w.max_parts = kMaxDenseParts;
     w.out_ids = (uint32_t *)out_ids.p;
     w.out_counts = (uint32_t *)out_counts.p;
     w.out_scores = scores ? (float *)out_scores.p : nullptr;

@@ -38,7 +38,7 @@ DeviceContext &device_context(int dev);
 struct Workspace {
     DevBuf item_off, dim, low, up, weight, weighted, k, out_off;
     DevBuf item_k0, item_nk, item_inc;
-    DevBuf span_start, span_len, inc, qinfo, work, ctr, qstate, done, part_cnt, scratch;
+    DevBuf span_start, span_len, inc, qinfo, work, ctr, qstate, done, lb, part_cnt, scratch;
     DevBuf out_ids, out_counts, out_scores;
     bool done_zeroed = false;
     int64_t done_q = 0;

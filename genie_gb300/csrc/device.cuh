@@ -16,7 +16,8 @@
 
 namespace gg {
 
-constexpr int kMaxParts = 16;        // id-range parts of one query
+constexpr int kMaxParts = 16;        // id-range parts of one sparse query
+constexpr int kMaxDenseParts = 64;   // id-range parts of one dense query (Work::max_parts bounds a search)
 constexpr int kMaxK = 2048;          // largest k per query
 constexpr int kItemChunk = 512;      // query items staged in shared memory at once
 constexpr int kCandCap = 2048;       // candidate buffer of the top-k selection
@@ -120,13 +121,15 @@ struct Work {
     int64_t *span_len;     // [units] its length (or segment count)
     uint32_t *inc;         // [units] increment per match
     QInfo *qinfo;          // [Q]
-    uint2 *work;           // [kNumLists][Q*kMaxParts] (query, part)
+    uint2 *work;           // [kNumLists][Q*kMaxParts] (query, part); a dense list holds (query, 0) once
     int64_t work_stride;   // Q*kMaxParts
     uint32_t *ctr;         // [kCtrWords]
     uint32_t *qstate;      // [Q] bit0: a sparse part overflowed
     uint32_t *done;        // [Q] finished parts
-    uint32_t *part_cnt;    // [Q*kMaxParts]
-    uint64_t *scratch;     // [sum(k)*kMaxParts] part results (keys)
+    uint32_t *lb;          // [Q] lower bound on the k-th primary of a dense query (from its finished tiles)
+    uint32_t *part_cnt;    // [Q*max_parts]
+    uint64_t *scratch;     // [sum(k)*max_parts] part results (keys)
+    int32_t max_parts;     // parts of a dense query (<= kMaxDenseParts); scratch stride per result slot
     uint32_t *out_ids;
     uint32_t *out_counts;
     float *out_scores;     // may be null

@@ -41,17 +41,14 @@ void read_oob(unsigned long long out[4]) {
 
 constexpr int kPlanThreads = 256;
 
-// Id-range parts of a dense query: one per dense_part_work posting ids, more
-// when the batch has too few queries to give every SM a part, at most one per
-// tile and kMaxParts.
-__device__ __forceinline__ int64_t dense_parts(int64_t total, int64_t ntiles, int64_t nq, const Tuning &T) {
-    int64_t pd = (total + T.dense_part_work - 1) / T.dense_part_work;
-    if (T.num_sms > 0 && nq > 0) {
-        const int64_t fill = (T.num_sms + nq - 1) / nq;
-        pd = pd > fill ? pd : fill;
-    }
-    pd = pd > ntiles ? ntiles : pd;
-    pd = pd > kMaxParts ? kMaxParts : pd;
+// Id-range parts of a dense query: one per counter tile, at most
+// W.max_parts (then a part sweeps several consecutive tiles).  Every dense
+// query of one counter width has the same number, so that the dense kernel
+// can take its work part-major (take_dense).
+__device__ __forceinline__ int64_t dense_parts(const DevIndex &ix, const Work &W, const Tuning &T, bool small) {
+    const int64_t tile = small ? T.dense_tile_u8 : T.dense_tile_u32;
+    const int64_t ntiles = (ix.n_objects + tile - 1) / tile;
+    const int64_t pd = ntiles < W.max_parts ? ntiles : W.max_parts;
     return pd < 1 ? 1 : pd;
 }
 
@@ -239,6 +236,7 @@ __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQuerie
     if (tid == 0) {
         W.done[q] = 0;
         W.qstate[q] = 0;
+        W.lb[q] = 0;
         if (k == 0 || k > (uint32_t)kMaxK) atomicOr(&W.ctr[kCtrError], kErrCapacity);
         const bool small = (qi.flags & kFlagSmallCount) != 0;
         const int64_t total = qi.total;
@@ -264,17 +262,17 @@ __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQuerie
                 list = packed ? kListSparsePacked : kListSparseWide;
             } else {
                 qi.cls = kClsDense;
-                const int64_t tile = small ? T.dense_tile_u8 : T.dense_tile_u32;
-                const int64_t ntiles = (ix.n_objects + tile - 1) / tile;
-                qi.parts = (uint16_t)dense_parts(total, ntiles, nq, T);
+                qi.parts = (uint16_t)dense_parts(ix, W, T, small);
                 list = small ? kListDenseSmall : kListDenseWide;
             }
         }
         W.qinfo[q] = qi;
         if (list >= 0) {
+            // a dense list holds the query once: its parts are taken part-major
+            const uint32_t entries = (list == kListDenseSmall || list == kListDenseWide) ? 1u : qi.parts;
             uint2 *wl = W.work + (size_t)list * W.work_stride;
-            uint32_t b = atomicAdd(&W.ctr[2 * list], (uint32_t)qi.parts);
-            for (uint32_t p = 0; p < qi.parts; ++p)
+            uint32_t b = atomicAdd(&W.ctr[2 * list], entries);
+            for (uint32_t p = 0; p < entries; ++p)
                 if (GG_OK(b + p, W.work_stride, 8)) wl[b + p] = make_uint2((uint32_t)q, p);
         }
     }
@@ -606,12 +604,28 @@ __device__ __forceinline__ uint32_t take_work(const Work &W, int list) {
     return w < n ? w : 0xFFFFFFFFu;
 }
 
+// Next (query, part) of a dense work list (P parts per query), part-major:
+// every query's part 0, then every query's part 1, ...  The CTAs running at
+// one time then count the same id range of different queries, and the slice
+// of the posting lists in that range (a fraction of the index that fits L2)
+// is read from HBM about once and from L2 by the other queries covering it.
+__device__ __forceinline__ bool take_dense(const Work &W, int list, uint32_t P, uint2 &out) {
+    const uint32_t nq = *(volatile uint32_t *)&W.ctr[2 * list];
+    const uint32_t n = nq * P;
+    if (*(volatile uint32_t *)&W.ctr[2 * list + 1] >= n) return false;
+    const uint32_t w = atomicAdd(&W.ctr[2 * list + 1], 1u);
+    if (w >= n) return false;
+    const uint32_t p = w / nq, i = w - p * nq;
+    out = make_uint2(W.work[(size_t)list * W.work_stride + i].x, p);
+    return true;
+}
+
 // Scratch / merge of a query's parts.  Part p of query q keeps its sorted
-// top-k keys in scratch[out_off*kMaxParts + p*k ..].
+// top-k keys in scratch[out_off*max_parts + p*k ..].
 struct MergeSet {
     const uint64_t *keys;
     const uint32_t *cnt;
-    uint32_t parts, k;
+    uint32_t parts, k, max_parts;
     template <class F>
     __device__ void for_each(F f) const {
         for (uint32_t p = 0; p < parts; ++p) {
@@ -619,7 +633,7 @@ struct MergeSet {
             for (uint32_t b = 0; b < n; b += blockDim.x) {
                 uint32_t i = b + threadIdx.x;
                 bool act = i < n;
-                act = act && GG_OK((size_t)p * k + i, (size_t)kMaxParts * k, 6);
+                act = act && GG_OK((size_t)p * k + i, (size_t)max_parts * k, 6);
                 uint64_t key = act ? __ldcg(keys + (size_t)p * k + i) : 0ull;
                 f(act, key_prim(key), key_id(key));
             }
@@ -630,19 +644,16 @@ struct MergeSet {
 __device__ void convert_to_dense(const DevIndex &ix, const Work &W, const Tuning &T, uint32_t q) {
     QInfo qi = W.qinfo[q];
     const bool small = (qi.flags & kFlagSmallCount) != 0;
-    const int64_t tile = small ? T.dense_tile_u8 : T.dense_tile_u32;
-    const int64_t ntiles = (ix.n_objects + tile - 1) / tile;
-    const int64_t pd = dense_parts(qi.total, ntiles, 1, T);
-    qi.parts = (uint16_t)pd;
+    qi.parts = (uint16_t)dense_parts(ix, W, T, small);
     qi.cls = kClsDense;
     W.qinfo[q] = qi;
     W.done[q] = 0;
     W.qstate[q] = 0;         // the dense parts' merge must not see the sparse overflow again
+    W.lb[q] = 0;
     const int list = small ? kListDenseSmall : kListDenseWide;
     uint2 *wl = W.work + (size_t)list * W.work_stride;
-    uint32_t base = atomicAdd(&W.ctr[2 * list], (uint32_t)pd);
-    for (uint32_t p = 0; p < pd; ++p)
-        if (GG_OK(base + p, W.work_stride, 13)) wl[base + p] = make_uint2(q, p);
+    const uint32_t at = atomicAdd(&W.ctr[2 * list], 1u);
+    if (GG_OK(at, W.work_stride, 13)) wl[at] = make_uint2(q, 0u);
 }
 
 // Finish one part: publish its keys, and let the last part merge them.
@@ -655,12 +666,13 @@ __device__ void finish_part(const DevIndex &ix, const Work &W, const Tuning &T, 
         write_results(W, out_off, qi.k, cand, n, weighted, qi.scale);
         return;
     }
-    uint64_t *dst = W.scratch + (size_t)out_off * kMaxParts + (size_t)p * qi.k;
+    const size_t mp = (size_t)W.max_parts;
+    uint64_t *dst = W.scratch + (size_t)out_off * mp + (size_t)p * qi.k;
     for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
-        if (GG_OK((size_t)out_off * kMaxParts + (size_t)p * qi.k + i, (size_t)W.out_cap * kMaxParts, 5))
+        if (GG_OK((size_t)out_off * mp + (size_t)p * qi.k + i, (size_t)W.out_cap * mp, 5))
             __stcg(dst + i, cand[i]);
     if (threadIdx.x == 0) {
-        __stcg(W.part_cnt + (size_t)q * kMaxParts + p, failed ? 0u : n);
+        __stcg(W.part_cnt + (size_t)q * mp + p, failed ? 0u : n);
         if (failed) atomicOr(&W.qstate[q], 1u);
     }
     __threadfence();
@@ -677,8 +689,8 @@ __device__ void finish_part(const DevIndex &ix, const Work &W, const Tuning &T, 
         __syncthreads();
         return;
     }
-    MergeSet ms{W.scratch + (size_t)out_off * kMaxParts, W.part_cnt + (size_t)q * kMaxParts,
-                qi.parts, qi.k};
+    MergeSet ms{W.scratch + (size_t)out_off * mp, W.part_cnt + (size_t)q * mp, qi.parts, qi.k,
+                (uint32_t)mp};
     const int bits = (qi.flags & kFlagSmallCount) ? 8 : 32;
     uint32_t nn = select_topk(ms, qi.k, bits, cand, kCandCap, ss);
     write_results(W, out_off, qi.k, cand, nn, weighted, qi.scale);
@@ -943,17 +955,21 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
     st.inc = (uint32_t *)(it_raw + kItemChunk * 20);
     st.flat = (uint32_t *)(it_raw + kItemChunk * 24);
     SelectScratch &ss = *(SelectScratch *)(it_raw + kItemChunk * 28 + 16);
-    __shared__ uint32_t s_work, s_nS, s_nc;
+    __shared__ uint32_t s_q, s_p, s_nS, s_nc, s_L;
 
     const int list = SMALL ? kListDenseSmall : kListDenseWide;
+    const uint32_t P_list = (uint32_t)dense_parts(ix, W, T, SMALL);
     for (;;) {
-        if (tid == 0) s_work = take_work(W, list);
+        if (tid == 0) {
+            uint2 wk;
+            if (!take_dense(W, list, P_list, wk)) wk.x = 0xFFFFFFFFu;
+            s_q = wk.x;
+            s_p = wk.y;
+        }
         __syncthreads();
-        const uint32_t w = s_work;
+        const uint32_t q = s_q, p = s_p;
         __syncthreads();
-        if (w == 0xFFFFFFFFu) break;
-        const uint2 wk = W.work[(size_t)list * W.work_stride + w];
-        const uint32_t q = wk.x, p = wk.y;
+        if (q == 0xFFFFFFFFu) break;
         if (!GG_OK(q, W.q_cap, 12)) continue;
         const QInfo qi = W.qinfo[q];
         const uint32_t P = qi.parts;
@@ -1022,14 +1038,20 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                 __syncthreads();
             }
             if (!any_ids) continue;
-            // merge this tile into the running top-k
-            const uint32_t nS = s_nS;
-            const uint32_t thr = nS == qi.k ? key_prim(S[qi.k - 1]) : 0u;
-            if (nS == qi.k) {
-                // S is full: a tile id enters only with a count above S's k-th
-                // (on a tie S's id, from an earlier tile, is smaller).  Few
-                // counters usually are: collect them behind a copy of S and
-                // sort the union.
+            // Merge this tile into the running top-k S.  A tile id enters
+            // with a primary above S's k-th once S is full (on a tie S's id,
+            // from an earlier tile of this part, is smaller), and never below
+            // L, the largest k-th primary a finished tile of another part of
+            // the query has found: the query's final k-th primary is at least
+            // L, so nothing below it can place.
+            if (tid == 0) s_L = *(volatile uint32_t *)&W.lb[q];
+            __syncthreads();
+            const uint32_t nS = s_nS, L = s_L;
+            uint32_t thr = nS == qi.k ? key_prim(S[qi.k - 1]) : 0u;
+            if (L > 0 && L - 1 > thr) thr = L - 1;
+            if (nS == qi.k || L > 0) {
+                // Few counters usually pass: collect them behind a copy of S
+                // and sort the union.
                 if (tid == 0) s_nc = 0;
                 for (uint32_t i = tid; i < nS; i += blockDim.x) cand[i] = S[i];
                 __syncthreads();
@@ -1068,8 +1090,13 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                     const uint32_t np2 = next_pow2(nS + m);
                     for (uint32_t i = nS + m + tid; i < np2; i += blockDim.x) cand[i] = 0ull;
                     bitonic_sort_desc(cand, np2);
-                    for (uint32_t i = tid; i < nS; i += blockDim.x) S[i] = cand[i];
+                    const uint32_t nk = min(nS + m, qi.k);
+                    for (uint32_t i = tid; i < nk; i += blockDim.x) S[i] = cand[i];
+                    if (tid == 0) s_nS = nk;
                     __syncthreads();
+                    // a full S raises the query's lower bound for its other parts
+                    if (tid == 0 && nk == qi.k && key_prim(S[qi.k - 1]) > L)
+                        atomicMax(&W.lb[q], key_prim(S[qi.k - 1]));
                     continue;
                 }
             }
@@ -1079,6 +1106,7 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                 if (GG_OK(i, kMaxK, 10)) S[i] = cand[i];
             if (tid == 0) s_nS = nn;
             __syncthreads();
+            if (tid == 0 && nn == qi.k && key_prim(S[qi.k - 1]) > L) atomicMax(&W.lb[q], key_prim(S[qi.k - 1]));
         }
         const uint32_t nS = s_nS;
         for (uint32_t i = tid; i < nS; i += blockDim.x) cand[i] = S[i];

@@ -32,7 +32,7 @@ constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
 // Byte layout of the workspace inside the array.
 struct NaLayout {
-    size_t item_k0, item_nk, item_inc, span_start, span_len, inc, qinfo, work, ctr, qstate, done,
+    size_t item_k0, item_nk, item_inc, span_start, span_len, inc, qinfo, work, ctr, qstate, done, lb,
         part_cnt, scratch, total;
 };
 
@@ -50,6 +50,7 @@ constexpr NaLayout na_layout() {
     L.ctr = o;        o += align256(kCtrWords * 4);
     L.qstate = o;     o += align256(kNaMaxQueries * 4);
     L.done = o;       o += align256(kNaMaxQueries * 4);
+    L.lb = o;         o += align256(kNaMaxQueries * 4);
     L.part_cnt = o;   o += align256(kNaMaxQueries * kMaxParts * 4);
     L.scratch = o;    o += align256(kNaMaxResults * kMaxParts * 8);
     L.total = o;
@@ -117,8 +118,10 @@ extern "C" int genie_search_noalloc(genie_index *ix, const genie_queries *q, con
     w.ctr = (uint32_t *)(base + kNa.ctr);
     w.qstate = (uint32_t *)(base + kNa.qstate);
     w.done = (uint32_t *)(base + kNa.done);
+    w.lb = (uint32_t *)(base + kNa.lb);
     w.part_cnt = (uint32_t *)(base + kNa.part_cnt);
     w.scratch = (uint64_t *)(base + kNa.scratch);
+    w.max_parts = kMaxParts;      // the fixed array holds 16 part results per result slot
     w.out_ids = out_ids;
     w.out_counts = out_counts;
     w.out_scores = out_scores;

@@ -48,7 +48,7 @@ struct Request {
 // Device-side state a request holds while in flight: its items and plan rows,
 // its k result slots, and the per-part keys of its top-k merge.
 int64_t request_bytes(int64_t items, uint32_t k) {
-    return items * 48 + (int64_t)k * (kMaxParts * 8 + 12) + 256;
+    return items * 48 + (int64_t)k * (kMaxDenseParts * 8 + 12) + 256;
 }
 
 struct Slot {
