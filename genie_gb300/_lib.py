@@ -52,11 +52,15 @@ PROTOTYPES = {
     "genie_last_error": (ctypes.c_char_p, []),
     "genie_version": (ctypes.c_int, []),
     "genie_init": (ctypes.c_int, [ctypes.c_int]),
+    "genie_device_reset": (ctypes.c_int, []),
     "genie_index_create": (ctypes.c_int, [P, I64, I32, P]),
     "genie_index_create_with": (ctypes.c_int, [P, I64, I32, I32, P]),
     "genie_index_create_bag": (ctypes.c_int, [P, P, I64, P]),
     "genie_index_create_compressed": (ctypes.c_int, [P, I64, I32, I32, I32, P]),
     "genie_index_destroy": (ctypes.c_int, [P]),
+    "genie_index_create_subsequence": (ctypes.c_int, [P, P, I64, P]),
+    "genie_index_subsequence_bits": (ctypes.c_int, [P, P]),
+    "genie_index_device_ids": (ctypes.c_int, [P, P]),
     "genie_index_get_info": (ctypes.c_int, [P, P]),
     "genie_index_copy_out": (ctypes.c_int, [P, P, P, P, P, P]),
     "genie_index_copy_compressed": (ctypes.c_int, [P, P, P, P, P, P]),

@@ -31,6 +31,11 @@ def _nvcc():
     return shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
 
 
+def cuda_home():
+    """The CUDA toolkit holding nvcc (its include/ and lib64/)."""
+    return os.path.dirname(os.path.dirname(os.path.realpath(_nvcc())))
+
+
 def sources():
     return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cc")))
 
@@ -87,9 +92,20 @@ def build(force=False, verbose=False):
     return LIB
 
 
+def cudart_link():
+    """Link flags of the CUDA runtime (the legacy interface's headers use it)."""
+    for d in ("lib64", "lib", os.path.join("targets", os.uname().machine + "-linux", "lib"),
+              os.path.join("targets", "sbsa-linux", "lib")):
+        p = os.path.join(cuda_home(), d)
+        if os.path.exists(os.path.join(p, "libcudart.so")):
+            return ["-L" + p, "-lcudart", "-Wl,-rpath," + p]
+    return ["-lcudart"]
+
+
 CPP = os.path.join(HERE, "cpp")
 CPP_LIB = os.path.join(HERE, "libgenie.so")
 SHIM_TEST = os.path.join(OBJ, "shim_test")
+LEGACY_TEST = os.path.join(OBJ, "legacy_test")
 
 
 def _cpp_fingerprint():
@@ -99,6 +115,7 @@ def _cpp_fingerprint():
     for d, _, fs in sorted(os.walk(inc)):
         files += [os.path.join(d, f) for f in sorted(fs) if f.endswith(".h")]
     files.append(os.path.join(ROOT, "tests", "cpp", "shim_test.cc"))
+    files.append(os.path.join(ROOT, "tests", "cpp", "legacy_test.cc"))
     for path in files:
         if os.path.exists(path):
             with open(path, "rb") as fh:
@@ -113,27 +130,28 @@ def build_cpp(force=False, verbose=False):
     cxx = shutil.which("g++") or "g++"
     fp = _cpp_fingerprint()
     stamp = os.path.join(OBJ, "cpp_fingerprint")
-    if not force and os.path.exists(CPP_LIB) and os.path.exists(SHIM_TEST) and os.path.exists(stamp):
+    if not force and all(os.path.exists(p) for p in (CPP_LIB, SHIM_TEST, LEGACY_TEST, stamp)):
         with open(stamp) as f:
             if f.read() == fp:
                 return CPP_LIB
     os.makedirs(OBJ, exist_ok=True)
-    inc = ["-I" + os.path.join(ROOT, "include")]
+    inc = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(cuda_home(), "include")]
     srcs = [os.path.join(CPP, f) for f in sorted(os.listdir(CPP)) if f.endswith(".cc")]
     steps = [
         [cxx, "-std=c++17", "-O2", "-fPIC", "-shared"] + inc + srcs +
-        ["-o", CPP_LIB + ".tmp", "-L" + HERE, "-lgenie_gb300", "-Wl,-rpath,$ORIGIN"],
+        ["-o", CPP_LIB + ".tmp", "-L" + HERE, "-lgenie_gb300", "-Wl,-rpath,$ORIGIN"] + cudart_link(),
     ]
     for cmd in steps:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("C++ interface build failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
     os.replace(CPP_LIB + ".tmp", CPP_LIB)
-    cmd = [cxx, "-std=c++17", "-O2"] + inc + [os.path.join(ROOT, "tests", "cpp", "shim_test.cc"), "-o", SHIM_TEST,
-           "-L" + HERE, "-lgenie", "-lgenie_gb300", "-Wl,-rpath,$ORIGIN/.."]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("C++ test build failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+    for src, exe in (("shim_test.cc", SHIM_TEST), ("legacy_test.cc", LEGACY_TEST)):
+        cmd = [cxx, "-std=c++17", "-O2"] + inc + [os.path.join(ROOT, "tests", "cpp", src), "-o", exe,
+               "-L" + HERE, "-lgenie", "-lgenie_gb300", "-Wl,-rpath,$ORIGIN/.."] + cudart_link()
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("C++ test build failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
     with open(stamp, "w") as f:
         f.write(fp)
     if verbose:

@@ -15,6 +15,7 @@
 #include <genie/genie.h>
 
 #include "../../include/genie_gb300.h"
+#include "flat_queries.h"
 
 #include <algorithm>
 #include <cmath>
@@ -117,29 +118,49 @@ void Config::DisplayConfiguration() {
 
 namespace table {
 
+inv_table::inv_table() {}
 inv_table::inv_table(const int32_t *values, int64_t n_objects, int32_t n_dims) {
-    throw_on_status(genie_index_create(values, n_objects, n_dims, &ix_));
+    genie_index *ix = nullptr;
+    throw_on_status(genie_index_create(values, n_objects, n_dims, &ix));
+    adopt(ix);
 }
-inv_table::inv_table(genie_index *adopt) : ix_(adopt) {}
+inv_table::inv_table(genie_index *ix) { adopt(ix); }
 inv_table::~inv_table() {
     if (ix_) genie_index_destroy(ix_);
 }
 
+void inv_table::adopt(genie_index *ix) {
+    if (ix_ && ix_ != ix) genie_index_destroy(ix_);
+    ix_ = ix;
+    d_inv_p = nullptr;
+    inv_host_.clear();
+    if (!ix_) return;
+    const uint32_t *ids = nullptr;
+    throw_on_status(genie_index_device_ids(ix_, &ids));
+    d_inv_p = (int *)ids;
+    int32_t bits = -1;
+    throw_on_status(genie_index_subsequence_bits(ix_, &bits));
+    shift_bits_subsequence = bits > 0 ? (unsigned)bits : 0u;
+}
+
 static genie_index_info info_of(genie_index *ix) {
     genie_index_info inf{};
+    if (!ix) throw exception::cpu_runtime_error("the table holds no index (load it first)");
     throw_on_status(genie_index_get_info(ix, &inf));
     return inf;
 }
 
-int inv_table::i_size() const { return (int)info_of(ix_).n_objects; }
+// rows of a subsequence table (its objects are rowID << bits | offset)
+int inv_table::i_size() const { return (int)(info_of(ix_).n_objects >> shift_bits_subsequence); }
 int inv_table::m_size() const { return (int)info_of(ix_).n_dims; }
 int64_t inv_table::inv_size() const { return info_of(ix_).n_ids; }
 
-std::vector<int> inv_table::inv() const {
+std::vector<int> *inv_table::inv() {
     const int64_t n = inv_size();
-    std::vector<uint32_t> ids((size_t)n);
-    throw_on_status(genie_index_copy_out(ix_, ids.data(), nullptr, nullptr, nullptr, nullptr));
-    return std::vector<int>(ids.begin(), ids.end());
+    inv_host_.resize((size_t)n);
+    static_assert(sizeof(int) == sizeof(uint32_t), "ids are copied as 32-bit words");
+    throw_on_status(genie_index_copy_out(ix_, (uint32_t *)inv_host_.data(), nullptr, nullptr, nullptr, nullptr));
+    return &inv_host_;
 }
 
 void inv_table::save(const std::string &filename) const { throw_on_status(genie_index_save(ix_, filename.c_str())); }
@@ -240,50 +261,6 @@ void ExecutionPolicy::SetNumOfQueries(const uint32_t num_of_queries) { num_of_qu
 uint32_t ExecutionPolicy::GetNumOfQueries() const { return num_of_queries_; }
 
 namespace {
-
-// Flattened genie_queries of a query list (arrays owned here).
-struct FlatQueries {
-    std::vector<int64_t> item_off{0};
-    std::vector<int32_t> dim, low, up;
-    std::vector<float> weight;
-    std::vector<uint8_t> weighted;
-    std::vector<uint32_t> k;
-    bool any_weighted = false;
-    int64_t total_k = 0;
-
-    explicit FlatQueries(const std::vector<query::Query> &qs) {
-        for (const query::Query &cq : qs) {
-            query::Query &q = const_cast<query::Query &>(cq);
-            std::vector<query::Query::range> rs;
-            q.dump(rs);
-            for (const auto &r : rs) {
-                dim.push_back(r.dim);
-                low.push_back(r.low);
-                up.push_back(r.up);
-                weight.push_back(r.weight);
-            }
-            item_off.push_back((int64_t)dim.size());
-            weighted.push_back(q.weighted() ? 1 : 0);
-            any_weighted = any_weighted || q.weighted();
-            if (q.topk() <= 0) throw exception::InvalidConfigurationException("a query has no top-k");
-            k.push_back((uint32_t)q.topk());
-            total_k += q.topk();
-        }
-    }
-    genie_queries view() const {
-        genie_queries g{};
-        g.n_queries = (int32_t)k.size();
-        g.item_off = item_off.data();
-        g.dim = dim.data();
-        g.low = low.data();
-        g.up = up.data();
-        g.weight = any_weighted ? weight.data() : nullptr;
-        g.weighted = any_weighted ? weighted.data() : nullptr;
-        g.k = k.data();
-        g.uniform_k = 0;
-        return g;
-    }
-};
 
 SearchResult to_result(const std::vector<uint32_t> &ids, const std::vector<uint32_t> &counts) {
     return SearchResult(std::vector<int>(ids.begin(), ids.end()), std::vector<int>(counts.begin(), counts.end()));

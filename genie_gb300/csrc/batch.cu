@@ -221,6 +221,10 @@ int genie_batch_create(genie_index *ix, const genie_batch_config *cfg, genie_bat
     *out = nullptr;
     if (cfg->max_queries <= 0 || cfg->max_items < 0 || cfg->max_k == 0 || cfg->max_k > (uint32_t)kMaxK)
         return fail(GENIE_ERR_INVALID_ARG, "batch capacity must hold >= 1 query and 1 <= max_k <= %d", kMaxK);
+    if (ix->sub_shift >= 0)
+        return fail(GENIE_ERR_NOT_IMPLEMENTED, "a subsequence index is searched through genie_search");
+    if ((int64_t)cfg->max_queries * kMaxDenseParts >= ((int64_t)1 << 32))
+        return fail(GENIE_ERR_INVALID_ARG, "at most %lld queries per batch", (long long)(((int64_t)1 << 32) / kMaxDenseParts - 1));
     cudaSetDevice(ix->device);
     genie_batch *b = new genie_batch();
     b->ix = ix;

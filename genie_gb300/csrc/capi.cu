@@ -49,11 +49,14 @@ void DevBuf::release() {
     bytes = 0;
 }
 
+namespace {
+DeviceContext g_ctx[64];
+std::mutex g_ctx_mu;
+}  // namespace
+
 DeviceContext &device_context(int dev) {
-    static DeviceContext ctx[64];
-    static std::mutex mu;
-    std::lock_guard<std::mutex> g(mu);
-    DeviceContext &c = ctx[dev & 63];
+    std::lock_guard<std::mutex> g(g_ctx_mu);
+    DeviceContext &c = g_ctx[dev & 63];
     if (!c.ready) {
         cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, dev);
         c.tuning = default_tuning();
@@ -104,7 +107,7 @@ void Workspace::release() {
     DevBuf *all[] = {&item_off, &dim, &low, &up, &weight, &weighted, &k, &out_off, &item_k0, &item_nk,
                      &item_inc, &span_start,
                      &span_len, &inc, &qinfo, &work, &ctr, &qstate, &done, &lb, &part_cnt, &scratch,
-                     &out_ids, &out_counts, &out_scores};
+                     &out_ids, &out_counts, &out_scores, &counters};
     for (DevBuf *b : all) b->release();
 }
 
@@ -277,6 +280,7 @@ int finish_loaded_index(genie_index *ix, genie_index **out) {
 
 int run_search(genie_index *ix, const genie_queries *q, const std::vector<int64_t> &out_off, int64_t n_items,
                uint32_t *out_ids, uint32_t *out_counts, float *out_scores, bool sync) {
+    if (ix->sub_shift >= 0) return subseq_search(ix, q, out_off, n_items, out_ids, out_counts, out_scores, sync);
     const int64_t Q = q->n_queries;
     const int64_t sumk = out_off[Q];
     Workspace &ws = ix->ws;
@@ -340,6 +344,18 @@ extern "C" {
 const char *genie_last_error(void) { return g_last_error.c_str(); }
 
 int genie_version(void) { return 1 * 10000 + 0 * 100 + 0; }
+
+int genie_device_reset(void) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const cudaError_t e = cudaDeviceReset();
+    {   // the kernels' shared-memory settings went with the context: prepare them again on next use
+        std::lock_guard<std::mutex> g(g_ctx_mu);
+        g_ctx[dev & 63] = DeviceContext();
+    }
+    noalloc_forget(dev);
+    return e ? cuda_fail(e, "cudaDeviceReset") : GENIE_OK;
+}
 
 int genie_init(int device) {
     int n = 0;
@@ -407,6 +423,12 @@ int genie_index_create_bag(const int32_t *values, const int64_t *row_off, int64_
     }
     ix->is_bag = true;
     return finish_index_create(ix, out);
+}
+
+int genie_index_device_ids(const genie_index *ix, const uint32_t **ids) {
+    if (!ix || !ids) return fail(GENIE_ERR_INVALID_ARG, "NULL argument");
+    *ids = ix->dev.ids;
+    return GENIE_OK;
 }
 
 int genie_index_destroy(genie_index *ix) {

@@ -40,6 +40,7 @@ struct Workspace {
     DevBuf item_k0, item_nk, item_inc;
     DevBuf span_start, span_len, inc, qinfo, work, ctr, qstate, done, lb, part_cnt, scratch;
     DevBuf out_ids, out_counts, out_scores;
+    DevBuf counters;                 // per-object counters of a subsequence search
     bool done_zeroed = false;
     int64_t done_q = 0;
     cudaError_t reserve(int64_t Q, int64_t items, int64_t units, int64_t sumk);
@@ -55,6 +56,11 @@ int batch_submit_async(genie_batch *b, const genie_queries *q, bool scores);
 int batch_ready(genie_batch *b);      // 1 done, 0 still running, < 0 a CUDA error
 int batch_collect(genie_batch *b, uint32_t *ids, uint32_t *counts, float *scores);
 int check_device_error(uint32_t err);
+// Drop the fixed workspace's cached device address of a device (after a reset).
+void noalloc_forget(int dev);
+// Search of a subsequence index (subseq.cu), on ix->stream; waits when sync.
+int subseq_search(genie_index *ix, const genie_queries *q, const std::vector<int64_t> &out_off, int64_t n_items,
+                  uint32_t *out_ids, uint32_t *out_counts, float *out_scores, bool sync);
 int64_t count_units(const HostIndex &h, const genie_queries *q);
 
 }  // namespace gg
@@ -72,6 +78,7 @@ int build_device_index(const int32_t *values, int64_t n, int32_t d, genie_index 
 struct genie_index {
     int device = 0;
     bool is_bag = false;
+    int32_t sub_shift = -1;          // subsequence index: ids are rowID << sub_shift | offset (-1: not one)
     gg::HostIndex host;              // host mirror: bounds and key offsets (ids live on the device)
     int64_t n_ids = 0;
     int32_t codec = 0;

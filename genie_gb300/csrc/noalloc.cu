@@ -69,6 +69,12 @@ std::mutex g_na_mu;
 void *g_na_ptr[64] = {};      // device address of g_search_scratch, per device
 
 }  // namespace
+
+void noalloc_forget(int dev) {
+    std::lock_guard<std::mutex> g(g_na_mu);
+    g_na_ptr[dev & 63] = nullptr;
+}
+
 }  // namespace gg
 
 using namespace gg;
@@ -86,6 +92,8 @@ extern "C" int genie_search_noalloc(genie_index *ix, const genie_queries *q, con
                     (long long)kNaMaxQueries, (long long)kNaMaxItems, (long long)kNaMaxResults, q->n_queries,
                     (long long)n_items, (long long)total_k, (size_t)kNaScratchBytes);
     if (q->n_queries == 0) return GENIE_OK;
+    if (ix->sub_shift >= 0)
+        return fail(GENIE_ERR_NOT_IMPLEMENTED, "a subsequence index is searched through genie_search");
     if (!q->item_off || !q->dim || !q->low || !q->up) return fail(GENIE_ERR_INVALID_ARG, "NULL query arrays");
     if (!q->k && (q->uniform_k == 0 || q->uniform_k > (uint32_t)kMaxK))
         return fail(GENIE_ERR_INVALID_ARG, "uniform k must be in [1, %d]", kMaxK);

@@ -165,6 +165,8 @@ using namespace gg;
 
 extern "C" int genie_index_save(const genie_index *ix, const char *path) {
     if (!ix || !path) return fail(GENIE_ERR_INVALID_ARG, "NULL argument");
+    if (ix->sub_shift >= 0)
+        return fail(GENIE_ERR_NOT_IMPLEMENTED, "the file format holds no subsequence index");
     return save_index(ix, path);
 }
 

@@ -9,6 +9,9 @@
 
 #include <genie/table/inv_table.h>
 
+typedef unsigned int u32;
+typedef unsigned long long u64;
+
 namespace genie {
 namespace query {
 

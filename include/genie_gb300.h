@@ -61,6 +61,11 @@ int genie_version(void);
 /* Select and initialise a device.  Replaces genie::utility::Init /
  * init_genie (src/genie/utility/init.cu:7-34). */
 int genie_init(int device);
+/* Reset the current device (cudaDeviceReset): every index, batch and server
+ * on it is invalid afterwards and must only be destroyed; the library
+ * prepares its kernels again on next use.  Replaces reset_device
+ * (original/interface.cc:910-913). */
+int genie_device_reset(void);
 
 /* ---------------------------------------------------------------- index */
 
@@ -105,6 +110,24 @@ int genie_index_create_bag(const int32_t *values, const int64_t *row_off,
  * Replaces inv_compr_table::build (table/inv_compr_table.cu:30-119). */
 int genie_index_create_compressed(const int32_t *values, int64_t n_objects, int32_t n_dims,
                                   int32_t codec, int32_t max_segment, genie_index **out);
+
+/* Subsequence index: rows of values (row r = values[row_off[r] ..
+ * row_off[r+1])); the object listed for the value at offset o of row r is
+ * r << bits | o, bits the least with 2^bits >= the longest row.  A search
+ * counts, for every (row, start offset) object, the items i of the query
+ * (i = the item's position in its query) whose range holds the row's value at
+ * start offset + i.  Searched through genie_search / genie_search_multi only.
+ * Replaces load_table_bijectMap with use_subsequence_search
+ * (original/interface.cc:650-655, table/inv_list.cc:193-235) and the match
+ * kernel's offset shift (matching/match.cu:84-94). */
+int genie_index_create_subsequence(const int32_t *values, const int64_t *row_off, int64_t n_rows,
+                                   genie_index **out);
+/* bits of a subsequence index (-1 for any other index): a result id is
+ * rowID << bits | offset (inv_table::_shift_bits_subsequence, inv_table.cu:202-205). */
+int genie_index_subsequence_bits(const genie_index *ix, int32_t *bits);
+/* Device address of the index's posting ids (read only; n_ids entries, valid
+ * while the index lives).  Replaces inv_table::d_inv_p (table/inv_table.h:55). */
+int genie_index_device_ids(const genie_index *ix, const uint32_t **ids);
 
 int genie_index_destroy(genie_index *ix);
 int genie_index_get_info(const genie_index *ix, genie_index_info *out);

@@ -222,3 +222,99 @@ def ref_codecs():
     r.ref_decode.restype = ctypes.c_int64
     r.ref_decode.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64]
     return r
+
+
+def _topk(counts, k):
+    """(ids, counts) of the k largest counts, ties by ascending id, padded (0, 0)."""
+    items = sorted(((c, i) for i, c in counts.items() if c > 0), key=lambda t: (-t[0], t[1]))[:k]
+    ids = [i for _, i in items] + [0] * (k - len(items))
+    cnt = [c for c, _ in items] + [0] * (k - len(items))
+    return ids, cnt
+
+
+def subsequence_search(rows, queries, k, radius=0):
+    """Subsequence search over rows of values, small cases only.  The object
+    of row r at offset o is r << bits | o, bits the least with 2^bits >= the
+    longest row (inv_list::invert_subsequence, table/inv_list.cc:193-235);
+    item j of a query ([v - radius, v + radius] of the query's j-th value)
+    adds 1 to object (r, s) when row r holds a value of that range at offset
+    s + j (the offset shift of match_AT, matching/match.cu:84-94).  Returns
+    (ids, counts) row-major, k slots per query."""
+    longest = max(len(r) for r in rows)
+    bits = 0
+    while (1 << bits) < longest:
+        bits += 1
+    out_ids, out_cnt = [], []
+    for q in queries:
+        counts = {}
+        for j, v in enumerate(q):
+            lo, hi = v - radius, v + radius
+            for r, row in enumerate(rows):
+                for p, x in enumerate(row):
+                    if p >= j and lo <= x <= hi:
+                        key = (r << bits) | (p - j)
+                        counts[key] = counts.get(key, 0) + 1
+        ids, cnt = _topk(counts, k)
+        out_ids += ids
+        out_cnt += cnt
+    return np.array(out_ids, np.int64), np.array(out_cnt, np.int64), bits
+
+
+def _grams(seq, base, g):
+    """sequence_to_gram for one sequence (original/interface.cc:930-975)."""
+    n = len(seq)
+    if n == 0:
+        return []
+    if n - g + 1 <= 0:
+        num = 0
+        for p in range(g):
+            num = num * base + (seq[p] if p < n else seq[0])
+        return [num]
+    out = []
+    for j in range(n - g + 1):
+        num = 0
+        for t in range(g):
+            num = num * base + seq[j + t]
+        out.append(num)
+    return out
+
+
+def _mark(grams, bits, keep_capped):
+    """The k-th repeat of a gram in one row marked in the low bits, capped at
+    2^bits - 1: kept at the cap on the table side (inv_list.cc:107-121),
+    dropped on the query side (original/interface.cc:552-566)."""
+    seen, out, cap = {}, [], (1 << bits) - 1
+    for x in grams:
+        if x not in seen:
+            seen[x] = 0
+            out.append(x << bits)
+        elif seen[x] < cap:
+            seen[x] += 1
+            out.append((x << bits) + seen[x])
+        elif keep_capped:
+            out.append((x << bits) + cap)
+    return out
+
+
+def sequence_search(rows, queries, k, gram_length=3, bits=6):
+    """Sequence (gram) search, small cases only: values reduced by the table
+    minimum, grams of gram_length values, repeats marked; the count of row r
+    is the number of the query's marked grams that r holds, with multiplicity
+    (load_table_sequence / load_query_sequence, original/interface.cc:519-616,
+    678-757).  Returns (ids, counts) row-major, k slots per query."""
+    mn = min(min(r) for r in rows if len(r))
+    mx = max(max(r) for r in rows if len(r))
+    base = mx - mn + 1
+    table = [_mark(_grams([v - mn for v in r], base, gram_length), bits, True) for r in rows]
+    out_ids, out_cnt = [], []
+    for q in queries:
+        qv = _mark(_grams([v - mn for v in q if mn <= v <= mx], base, gram_length), bits, False)
+        counts = {}
+        for r, marked in enumerate(table):
+            c = sum(marked.count(v) for v in qv)
+            if c:
+                counts[r] = c
+        ids, cnt = _topk(counts, k)
+        out_ids += ids
+        out_cnt += cnt
+    return np.array(out_ids, np.int64), np.array(out_cnt, np.int64)

@@ -100,7 +100,7 @@ static int gpu_checks(const std::string &table_csv, const std::string &query_csv
     // binary save / load gives the same answers
     SaveTableToBinary(dir + "/table.bin", table);
     std::shared_ptr<table::inv_table> loaded = LoadTableFromBinary(dir + "/table.bin");
-    CHECK(loaded->inv() == table->inv());
+    CHECK(*loaded->inv() == *table->inv());
     std::vector<query::Query> q2 = BuildQuery(policy, loaded, query_data);
     CHECK(Match(policy, loaded, q2) == r1);
 
