@@ -70,6 +70,9 @@ PROTOTYPES = {
     "genie_index_load": (ctypes.c_int, [ctypes.c_char_p, P]),
     "genie_search": (ctypes.c_int, [P, P, P, P, P]),
     "genie_search_multi": (ctypes.c_int, [P, P, I32, P, P, P]),
+    "genie_codec_set_match": (ctypes.c_int, [I32, P, P]),
+    "genie_codec_get_match": (ctypes.c_int, [I32, P, P]),
+    "genie_match_builtin": (ctypes.c_int, [P, P, P, P, P]),
     "genie_search_noalloc": (ctypes.c_int, [P, P, P, I64, I64, P, P, P, P]),
     "genie_batch_create": (ctypes.c_int, [P, P, P]),
     "genie_batch_destroy": (ctypes.c_int, [P]),

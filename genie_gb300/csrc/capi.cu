@@ -482,8 +482,64 @@ int genie_index_adaptive_range(const genie_index *ix, int32_t dim, float selecti
     return GENIE_OK;
 }
 
+// ---------------------------------------------------------------- match registry
+//
+// The match function of each codec id, as the reference keeps a
+// COMPRESSION_TYPE -> MatchIntegratedFunPtr map (compression/
+// DeviceCodecFactory.h:23-30, DeviceCodecFactory.cu:48-70) that knn() looks up
+// for a table's codec (matching/knn.cu:130-140).  An empty entry means the
+// built-in path (plain kernels, or the fused warp decoders of the codec).
+
+namespace {
+struct MatchEntry {
+    genie_match_fn fn = nullptr;
+    void *user = nullptr;
+};
+MatchEntry g_match[GENIE_N_CODECS];
+std::mutex g_match_mu;
+
+bool registered_match(int32_t codec, MatchEntry &out) {
+    if (codec < 0 || codec >= GENIE_N_CODECS) return false;
+    std::lock_guard<std::mutex> g(g_match_mu);
+    out = g_match[codec];
+    return out.fn != nullptr;
+}
+}  // namespace
+
+int genie_codec_set_match(int32_t codec, genie_match_fn fn, void *user) {
+    if (codec < 0 || codec >= GENIE_N_CODECS) return fail(GENIE_ERR_INVALID_ARG, "unknown codec %d", codec);
+    std::lock_guard<std::mutex> g(g_match_mu);
+    g_match[codec].fn = fn;
+    g_match[codec].user = fn ? user : nullptr;
+    return GENIE_OK;
+}
+
+int genie_codec_get_match(int32_t codec, genie_match_fn *fn, void **user) {
+    if (codec < 0 || codec >= GENIE_N_CODECS) return fail(GENIE_ERR_INVALID_ARG, "unknown codec %d", codec);
+    std::lock_guard<std::mutex> g(g_match_mu);
+    if (fn) *fn = g_match[codec].fn;
+    if (user) *user = g_match[codec].user;
+    return GENIE_OK;
+}
+
+int genie_match_builtin(genie_index *ix, const genie_queries *q, uint32_t *out_ids, uint32_t *out_counts,
+                        float *out_scores) {
+    if (!ix) return fail(GENIE_ERR_INVALID_ARG, "index is NULL");
+    std::vector<int64_t> out_off;
+    int64_t n_items = 0;
+    int rc = validate_queries(q, out_off, n_items);
+    if (rc) return rc;
+    if (q->n_queries == 0) return GENIE_OK;
+    if (!out_ids || !out_counts) return fail(GENIE_ERR_INVALID_ARG, "output buffers are NULL");
+    std::lock_guard<std::mutex> g(ix->mu);
+    cudaSetDevice(ix->device);
+    return run_search(ix, q, out_off, n_items, out_ids, out_counts, out_scores, true);
+}
+
 int genie_search(genie_index *ix, const genie_queries *q, uint32_t *out_ids, uint32_t *out_counts, float *out_scores) {
     if (!ix) return fail(GENIE_ERR_INVALID_ARG, "index is NULL");
+    MatchEntry m;
+    if (registered_match(ix->codec, m)) return m.fn(ix, q, out_ids, out_counts, out_scores, m.user);
     std::vector<int64_t> out_off;
     int64_t n_items = 0;
     int rc = validate_queries(q, out_off, n_items);
@@ -506,21 +562,31 @@ int genie_search_multi(genie_index *const *ixs, const genie_queries *qs, int32_t
         if (rc) return rc;
         base[i + 1] = base[i] + offs[i].back();
     }
-    // every index runs on its own stream; all batches are in flight together
+    // indexes whose codec has a registered match function run it first
+    std::vector<char> custom(n_index, 0);
     for (int32_t i = 0; i < n_index; ++i) {
-        if (qs[i].n_queries == 0) continue;
+        MatchEntry m;
+        if (qs[i].n_queries == 0 || !registered_match(ixs[i]->codec, m)) continue;
+        custom[i] = 1;
+        int rc = m.fn(ixs[i], &qs[i], out_ids + base[i], out_counts + base[i], out_scores ? out_scores + base[i] : nullptr,
+                      m.user);
+        if (rc) return rc;
+    }
+    // every other index runs on its own stream; all batches are in flight together
+    for (int32_t i = 0; i < n_index; ++i) {
+        if (qs[i].n_queries == 0 || custom[i]) continue;
         ixs[i]->mu.lock();
         cudaSetDevice(ixs[i]->device);
         int rc = run_search(ixs[i], &qs[i], offs[i], items[i], out_ids + base[i], out_counts + base[i],
                             out_scores ? out_scores + base[i] : nullptr, false);
         if (rc) {
-            for (int32_t j = 0; j <= i; ++j) if (qs[j].n_queries) ixs[j]->mu.unlock();
+            for (int32_t j = 0; j <= i; ++j) if (qs[j].n_queries && !custom[j]) ixs[j]->mu.unlock();
             return rc;
         }
     }
     int rc = GENIE_OK;
     for (int32_t i = 0; i < n_index; ++i) {
-        if (qs[i].n_queries == 0) continue;
+        if (qs[i].n_queries == 0 || custom[i]) continue;
         cudaError_t e = cudaStreamSynchronize(ixs[i]->stream);
         if (e && !rc) rc = cuda_fail(e, "multi-index search");
         if (!rc) rc = check_device_error(*ixs[i]->host_err);

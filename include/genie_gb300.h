@@ -188,6 +188,23 @@ typedef struct {
 int genie_search(genie_index *ix, const genie_queries *q, uint32_t *out_ids,
                  uint32_t *out_counts, float *out_scores);
 
+/* Plugin point: the match function genie_search and genie_search_multi use
+ * for the indexes of one codec id (0 = uncompressed), as the reference
+ * registers a MatchIntegratedFunPtr per COMPRESSION_TYPE
+ * (compression/DeviceCodecFactory.h:23-30, DeviceCodecFactory.cu:48-70,
+ * looked up in matching/knn.cu:130-140).  A function takes the arguments of
+ * genie_search plus the user pointer it was registered with, fills the
+ * outputs in the genie_search layout and returns a status.  With no function
+ * registered (the default, or fn = NULL) the built-in path runs, which a
+ * registered function may call itself through genie_match_builtin.  Batched
+ * and served searches always run the built-in kernels. */
+typedef int (*genie_match_fn)(genie_index *ix, const genie_queries *q, uint32_t *out_ids, uint32_t *out_counts,
+                              float *out_scores, void *user);
+int genie_codec_set_match(int32_t codec, genie_match_fn fn, void *user);
+int genie_codec_get_match(int32_t codec, genie_match_fn *fn, void **user);
+int genie_match_builtin(genie_index *ix, const genie_queries *q, uint32_t *out_ids, uint32_t *out_counts,
+                        float *out_scores);
+
 /* Multi-index search, one query batch per index, results concatenated in
  * index order.  Replaces knn_search_MT / knn_MT
  * (original/interface.cc:859-909, matching/knn.cu:185-283). */
