@@ -40,6 +40,10 @@ class GenieServerConfig(ctypes.Structure):
                 ("window_us", I32), ("memory_budget", I64)]
 
 
+class GenieRequestRouter(ctypes.Structure):
+    _fields_ = [("server", P), ("n_clusters", I32), ("index_id", P), ("id_offset", P), ("radius", I32)]
+
+
 class GenieServerReport(ctypes.Structure):
     _fields_ = [("submitted", I64), ("completed", I64), ("rejected", I64), ("batches", I64),
                 ("mean_batch", ctypes.c_double), ("p50_us", ctypes.c_double), ("p99_us", ctypes.c_double),
@@ -97,6 +101,11 @@ PROTOTYPES = {
     "genie_server_reset_stats": (ctypes.c_int, [P]),
     "genie_server_now_ns": (I64, []),
     "genie_server_destroy": (ctypes.c_int, [P]),
+    "genie_request_handle": (ctypes.c_int, [P, ctypes.c_char_p, P, I64, P]),
+    "genie_request_listen": (ctypes.c_int, [P, ctypes.c_char_p, I32, P]),
+    "genie_request_listener_port": (ctypes.c_int, [P, P]),
+    "genie_request_listener_handled": (ctypes.c_int, [P, P]),
+    "genie_request_listener_stop": (ctypes.c_int, [P]),
     "genie_merge_shards": (ctypes.c_int, [I32, P, P, P, P, I32, P, U32, P, P, P]),
     "genie_codec_encode": (I64, [I32, P, I64, P, I64]),
     "genie_codec_encode_bound": (I64, [I64]),

@@ -349,6 +349,42 @@ int genie_server_reset_stats(genie_server *s);
 int64_t genie_server_now_ns(void);
 int genie_server_destroy(genie_server *s);
 
+/* ---------------------------------------------------------------- requests */
+
+/* The request protocol over a server: a request is one JSON document
+ *   {"topk": K, "queries": [{"content": [v0, v1, ...], "clusters": [c, ...]}, ...]}
+ * in which value j of a query's content is item j (dim j, values
+ * [v - radius, v + radius]) and the query is searched on every cluster it
+ * names.  The answer is
+ *   {"topk": K, "results": [{"ids": [...], "counts": [...]}, ...]}
+ * with K slots per query, the clusters' answers merged by (count desc, id
+ * asc) after adding each cluster's id offset, padded (0, 0); an invalid
+ * request is answered {"error": "..."} with the reference's messages.
+ * Replaces dist_genie's request parser, listener, per-cluster search and
+ * merge (dist_genie/parser.cu:128-216, scheduler.cc:20-64, search.cu:34-52,
+ * sorting.cc:20-64), which wrote the answer to a file instead. */
+typedef struct genie_request_listener genie_request_listener;
+typedef struct {
+    genie_server *server;       /* a started server holding the clusters' indexes */
+    int32_t n_clusters;
+    const int32_t *index_id;    /* server index id of each cluster */
+    const int64_t *id_offset;   /* global id of each cluster's object 0 */
+    int32_t radius;             /* half-width of every item's value range */
+} genie_request_router;
+
+/* Answer one request document (no socket): the answer (NUL-terminated) goes
+ * to out; *out_len receives its length even when out_cap is too small. */
+int genie_request_handle(const genie_request_router *router, const char *json, char *out, int64_t out_cap,
+                         int64_t *out_len);
+/* Listen on host:port (port 0: any free port) on a thread of its own; each
+ * connection carries one request, read until the client shuts its side, and
+ * gets the answer back before the connection closes. */
+int genie_request_listen(const genie_request_router *router, const char *host, int32_t port,
+                         genie_request_listener **out);
+int genie_request_listener_port(const genie_request_listener *l, int32_t *port);
+int genie_request_listener_handled(const genie_request_listener *l, int64_t *n);
+int genie_request_listener_stop(genie_request_listener *l);
+
 /* ---------------------------------------------------------------- shards */
 
 /* Merge the per-shard results of an id-range sharded search: shard s holds
