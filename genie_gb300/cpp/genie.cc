@@ -22,7 +22,9 @@
 #include <cstdio>
 #include <fstream>
 #include <iostream>
+#include <iterator>
 #include <sstream>
+#include <thread>
 
 namespace genie {
 
@@ -364,19 +366,55 @@ std::shared_ptr<ExecutionPolicy> MakePolicy(const Config &config) {
 
 // ---------------------------------------------------------------- I/O
 
+// Integers of one line, separated by ',' or blanks (FileReader.cc:54-83).
+static void parse_line(const char *p, const char *e, std::vector<int> &row) {
+    auto sep = [](char c) { return c == ',' || c == ' ' || c == '\t' || c == '\r' || c == '\n'; };
+    while (p < e) {
+        while (p < e && sep(*p)) ++p;
+        if (p >= e) break;
+        const char *q = p;
+        long long v = 0;
+        bool neg = false;
+        if (*q == '-' || *q == '+') neg = *q++ == '-';
+        const char *d = q;
+        while (q < e && *q >= '0' && *q <= '9') v = v * 10 + (*q++ - '0');
+        if (q > d) row.push_back((int)(neg ? -v : v));
+        while (q < e && !sep(*q)) ++q;          // the rest of a token that is not a number
+        p = q;
+    }
+}
+
+// The first `limit` lines (all when < 0) of a CSV file as rows of integers.
+// The file is read at once and its lines are parsed in parallel, one block
+// of lines per host thread.
 static std::vector<std::vector<int> > read_rows(const std::string &filename, long long limit) {
     std::vector<std::vector<int> > rows;
-    std::ifstream in(filename);
+    std::ifstream in(filename, std::ios::binary);
     if (!in) return rows;
-    std::string line;
-    while ((limit < 0 || (long long)rows.size() < limit) && std::getline(in, line)) {
-        std::replace(line.begin(), line.end(), ',', ' ');
-        std::istringstream ss(line);
-        std::vector<int> row;
-        long long v;
-        while (ss >> v) row.push_back((int)v);
-        rows.push_back(std::move(row));
+    std::string text((std::istreambuf_iterator<char>(in)), std::istreambuf_iterator<char>());
+    std::vector<size_t> starts;
+    for (size_t i = 0; i < text.size(); ++i) {
+        if (i == 0 || text[i - 1] == '\n') {
+            if (limit >= 0 && (long long)starts.size() >= limit) break;
+            starts.push_back(i);
+        }
     }
+    const size_t n = starts.size();
+    rows.resize(n);
+    auto line_end = [&](size_t r) {
+        if (r + 1 < n) return starts[r + 1];
+        const size_t nl = text.find('\n', starts[r]);
+        return nl == std::string::npos ? text.size() : nl + 1;
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = std::min<size_t>(hw, std::max<size_t>(1, n / 4096));
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < nt; ++t)
+        th.emplace_back([&, t] {
+            for (size_t r = n * t / nt; r < n * (t + 1) / nt; ++r)
+                parse_line(text.data() + starts[r], text.data() + line_end(r), rows[r]);
+        });
+    for (auto &x : th) x.join();
     return rows;
 }
 

@@ -79,7 +79,7 @@ int enqueue(genie_batch *b, cudaStream_t s) {
     const Work w = b->ws.view(b->cfg.max_queries, true);
     if (!b->cfg.use_graph) {
         // direct launches, with an event after every stage for per-kernel timing
-        b->last_kernels = launch_match(b->ix->dev, q, w, b->tuning, ctx.num_sms, s, b->stage_ev);
+        b->last_kernels = launch_match(index_view(b->ix, b->tuning), q, w, b->tuning, ctx.num_sms, s, b->stage_ev);
         cudaError_t e = cudaGetLastError();
         return e ? cuda_fail(e, "batch launch") : GENIE_OK;
     }
@@ -87,9 +87,10 @@ int enqueue(genie_batch *b, cudaStream_t s) {
         if (b->gexec) cudaGraphExecDestroy(b->gexec);
         b->gexec = nullptr;
         cudaGraph_t g = nullptr;
+        const DevIndex d = index_view(b->ix, b->tuning);     // directories built before the capture
         cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
         if (e) return cuda_fail(e, "graph capture");
-        b->last_kernels = launch_match(b->ix->dev, q, w, b->tuning, ctx.num_sms, b->stream);
+        b->last_kernels = launch_match(d, q, w, b->tuning, ctx.num_sms, b->stream);
         cudaError_t le = cudaGetLastError();
         e = cudaStreamEndCapture(b->stream, &g);
         if (le) {

@@ -83,6 +83,7 @@ cudaError_t Workspace::reserve(int64_t Q, int64_t items, int64_t units, int64_t 
     RES(span_start, units * 8 + 16);
     RES(span_len, units * 8 + 16);
     RES(inc, units * 4 + 16);
+    RES(unit_key, units * 4 + 16);
     RES(qinfo, Q * sizeof(QInfo) + 16);
     RES(work, (size_t)kNumLists * Q * kMaxParts * sizeof(uint2) + 16);
     RES(ctr, kCtrWords * 4);
@@ -107,7 +108,7 @@ void Workspace::release() {
     DevBuf *all[] = {&item_off, &dim, &low, &up, &weight, &weighted, &k, &out_off, &item_k0, &item_nk,
                      &item_inc, &span_start,
                      &span_len, &inc, &qinfo, &work, &ctr, &qstate, &done, &lb, &part_cnt, &scratch,
-                     &out_ids, &out_counts, &out_scores, &counters};
+                     &out_ids, &out_counts, &out_scores, &counters, &unit_key};
     for (DevBuf *b : all) b->release();
 }
 
@@ -119,6 +120,7 @@ Work Workspace::view(int64_t Q, bool scores) const {
     w.span_start = (int64_t *)span_start.p;
     w.span_len = (int64_t *)span_len.p;
     w.inc = (uint32_t *)inc.p;
+    w.unit_key = (uint32_t *)unit_key.p;
     w.qinfo = (QInfo *)qinfo.p;
     w.work = (uint2 *)work.p;
     w.work_stride = Q * kMaxParts;
@@ -314,7 +316,7 @@ int run_search(genie_index *ix, const genie_queries *q, const std::vector<int64_
     dq.dyn = nullptr;
     Work w = ws.view(Q, out_scores != nullptr);
     DeviceContext &ctx = device_context(ix->device);
-    ix->last_launches = launch_match(ix->dev, dq, w, ix->tuning, ctx.num_sms, s);
+    ix->last_launches = launch_match(index_view(ix, ix->tuning), dq, w, ix->tuning, ctx.num_sms, s);
     if ((e = cudaGetLastError())) return cuda_fail(e, "match launch");
     if ((e = cudaMemcpyAsync(ix->host_err, w.ctr + kCtrError, 4, cudaMemcpyDeviceToHost, s))) return cuda_fail(e, "error word");
     if ((e = cudaMemcpyAsync(out_ids, w.out_ids, sumk * 4, cudaMemcpyDeviceToHost, s))) return cuda_fail(e, "result ids");
@@ -336,6 +338,12 @@ genie_index::~genie_index() {
     d_ids.release(); d_key_off.release(); d_key_base.release(); d_dim_min.release(); d_dim_max.release();
     d_words.release(); d_key_seg.release(); d_seg_word_off.release(); d_seg_first.release(); d_seg_len.release();
     ws.release();
+    d_dir_slot.release();
+    d_dir_row_key.release();
+    for (auto &d : dirs) {
+        d.second->release();
+        delete d.second;
+    }
     if (host_err) cudaFreeHost(host_err);
 }
 

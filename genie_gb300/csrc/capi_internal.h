@@ -41,6 +41,7 @@ struct Workspace {
     DevBuf span_start, span_len, inc, qinfo, work, ctr, qstate, done, lb, part_cnt, scratch;
     DevBuf out_ids, out_counts, out_scores;
     DevBuf counters;                 // per-object counters of a subsequence search
+    DevBuf unit_key;
     bool done_zeroed = false;
     int64_t done_q = 0;
     cudaError_t reserve(int64_t Q, int64_t items, int64_t units, int64_t sumk);
@@ -49,6 +50,10 @@ struct Workspace {
 };
 
 int validate_queries(const genie_queries *q, std::vector<int64_t> &out_off, int64_t &n_items);
+
+// The device view of an index for a tuning: ix->dev plus the tile
+// directories of the tuning's two tile sizes (built on first use).
+DevIndex index_view(genie_index *ix, const Tuning &t);
 
 // Asynchronous steps of one batch for the serving loop (batch.cu): stage,
 // launch and download on the batch's own stream; poll; copy the results out.
@@ -89,6 +94,13 @@ struct genie_index {
     gg::DevBuf d_words, d_key_seg, d_seg_word_off, d_seg_first, d_seg_len;
     gg::DevIndex dev{};
     gg::Tuning tuning{};
+    // tile directories (tile_dir.cu), built on first use per tile size and
+    // kept while the index lives
+    std::mutex dir_mu;
+    bool dir_rows_ready = false;
+    int64_t dir_rows = -1;
+    gg::DevBuf d_dir_slot, d_dir_row_key;
+    std::vector<std::pair<int32_t, gg::DevBuf *>> dirs;
     cudaStream_t stream = nullptr;
     std::mutex mu;                   // serialises searches on this handle's workspace
     gg::Workspace ws;

@@ -54,6 +54,15 @@ struct DevIndex {
     const int64_t *seg_word_off;   // [n_segs+1] first word of each segment
     const uint32_t *seg_first;     // [n_segs] first id of each segment (skip pointer)
     const int64_t *seg_pos;        // [n_segs+1] posting position of each segment
+    // tile directories (tile_dir.cu): dir_slot[key] = row of a long list (~0u:
+    // none); row r of dir8 / dir32 holds, for the tiles of dir8_tile /
+    // dir32_tile ids, the offset in the list of its first id (segment) at or
+    // past each tile boundary, ntiles + 1 entries.  Null / 0 when absent.
+    const uint32_t *dir_slot;
+    const uint32_t *dir8;
+    const uint32_t *dir32;
+    int32_t dir8_tile;
+    int32_t dir32_tile;
 };
 
 struct DevQueries {
@@ -120,6 +129,7 @@ struct Work {
     int64_t *span_start;   // [units] start of the unit's sorted list (or first segment)
     int64_t *span_len;     // [units] its length (or segment count)
     uint32_t *inc;         // [units] increment per match
+    uint32_t *unit_key;    // [units] (dim,value) key of the unit's list (null: not written)
     QInfo *qinfo;          // [Q]
     uint2 *work;           // [kNumLists][Q*kMaxParts] (query, part); a dense list holds (query, 0) once
     int64_t work_stride;   // Q*kMaxParts

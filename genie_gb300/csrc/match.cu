@@ -146,6 +146,7 @@ __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQuerie
             W.span_start[i] = a;
             W.span_len[i] = e - a;
             W.inc[i] = inc;
+            if (W.unit_key) W.unit_key[i] = (uint32_t)k0;
         }
         if (nk > 1) s_multi = 1;
         if (i == i0 + tid) {
@@ -203,6 +204,7 @@ __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQuerie
                     W.span_start[base + ex] = a_first;
                     W.span_len[base + ex] = e_first - a_first;
                     W.inc[base + ex] = inc;
+                    if (W.unit_key) W.unit_key[base + ex] = (uint32_t)k0;
                 }
                 nk = 0;
             }
@@ -214,6 +216,7 @@ __global__ void __launch_bounds__(kPlanThreads, 8) k_plan(DevIndex ix, DevQuerie
                 W.span_start[u] = a;
                 W.span_len[u] = e - a;
                 W.inc[u] = inc;
+                if (W.unit_key) W.unit_key[u] = (uint32_t)key;
             }
             base += tot;
         }
@@ -507,6 +510,104 @@ __device__ __forceinline__ void stream_runs(const uint32_t *__restrict__ ids, co
                 for (int r = 0; r < R; ++r)
                     if (32 * (g + r) + lane < n) visit(v[r], inc);
             }
+        }
+    }
+}
+
+// Compressed lists in runs (the dense kernel): warp tasks of up to kSegRun
+// consecutive segments of one staged unit.  The item lookup and the
+// segments' word offsets and lengths are loaded once per task (one lane per
+// segment).  A full 128-id segment of a BP32-based codec (BP32,
+// SERIAL_DELTA_BP32, SERIAL_DELTA_COMP_BP32_COPY/VARINT: one 128-value BP32
+// block, no tail) is unpacked straight from the words: lane l reads the one
+// or two words holding its four values of miniblock l/8 (L1 hits after the
+// first lane), extracts them with shifts, and the delta stage is one warp
+// prefix sum.  Other segments (list tails, other codecs) take the generic
+// warp decoder.  Ids outside [lo, hi) are skipped.
+constexpr uint32_t kSegRun = 8;
+constexpr uint32_t kBlockIds = 128;
+
+// Whether a codec's full segments are one bare BP32 block (after an optional
+// composite length word), and its delta stages.
+__host__ __device__ __forceinline__ bool bp32_block_codec(int codec, int &deltas, bool &len_word) {
+    int inner = 0;
+    codec_parts(codec, deltas, inner);
+    len_word = inner == kInnerCompCopy || inner == kInnerCompVarint;
+    return (inner == kInnerBP32 || len_word) && (deltas == 0 || deltas == 1);
+}
+
+template <class V>
+__device__ __forceinline__ void stream_segment_runs(const DevIndex &ix, const ItemStage &st, uint32_t n_items,
+                                                    uint32_t n_tasks, uint32_t lo, uint32_t hi, V &&visit) {
+    int deltas = 0;
+    bool len_word = false;
+    const bool fast_codec = bp32_block_codec(ix.codec, deltas, len_word);
+    const uint32_t lane = lane_id(), nw = blockDim.x >> 5;
+    for (uint32_t f = warp_id(); f < n_tasks; f += nw) {
+        uint32_t a = 0, b = n_items;      // last unit with flat <= f
+        while (a < b) {
+            const uint32_t mid = (a + b + 1) >> 1;
+            if (st.flat[mid] <= f) a = mid; else b = mid - 1;
+        }
+        const uint32_t r0 = (f - st.flat[a]) * kSegRun;
+        const uint32_t ns = min(kSegRun, st.len[a] - r0);
+        const uint32_t inc = st.inc[a];
+        const int64_t s0 = st.start[a] + r0;
+        // word offset and posting position of segments s0 .. s0+ns (one per lane)
+        int64_t wo = 0, sp = 0;
+        if (lane <= ns) {
+            wo = __ldg(ix.seg_word_off + s0 + lane);
+            sp = __ldg(ix.seg_pos + s0 + lane);
+        }
+        for (uint32_t j = 0; j < ns; ++j) {
+            const int64_t w0 = __shfl_sync(0xffffffffu, wo, j), w1 = __shfl_sync(0xffffffffu, wo, j + 1);
+            const int64_t n = __shfl_sync(0xffffffffu, sp, j + 1) - __shfl_sync(0xffffffffu, sp, j);
+            if (!(fast_codec && n == (int64_t)kBlockIds)) {
+                auto v = [&](uint32_t id, uint32_t) {
+                    if (id >= lo && id < hi) visit(id, inc);
+                };
+                decode_segment_values(ix.codec, ix.words, w0, w1, v);
+                continue;
+            }
+            // [len1] [n = 128] [widths] [miniblock 0] .. [miniblock 3]
+            const uint32_t *w = ix.words + w0 + (len_word ? 1 : 0);
+            const uint32_t hdr = __ldg(w + 1);
+            const uint32_t m = lane >> 3;
+            const uint32_t b = (hdr >> (24 - 8 * m)) & 255u;
+            const uint32_t before = (m > 0 ? (hdr >> 24) : 0u) + (m > 1 ? (hdr >> 16) & 255u : 0u) +
+                                    (m > 2 ? (hdr >> 8) & 255u : 0u);
+            const uint32_t *mb = w + 2 + before;
+            const uint32_t j0 = (lane & 7u) * 4u;
+            const uint32_t mask = b >= 32 ? 0xFFFFFFFFu : (1u << b) - 1u;
+            uint32_t v[4];
+            if (b <= 8) {       // the four values lie in one 64-bit window
+                const uint32_t bit0 = j0 * b, wi = bit0 >> 5, sh = bit0 & 31u;
+                const uint32_t lo_w = b ? __ldg(mb + wi) : 0u;
+                const uint32_t hi_w = (b && sh + 4 * b > 32) ? __ldg(mb + wi + 1) : 0u;
+                const uint64_t win = (((uint64_t)hi_w << 32) | lo_w) >> sh;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) v[k] = (uint32_t)(win >> (k * b)) & mask;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const uint32_t bit = (j0 + k) * b, wi = bit >> 5, sh = bit & 31u;
+                    const uint32_t lo_w = __ldg(mb + wi);
+                    const uint32_t hi_w = sh + b > 32 ? __ldg(mb + wi + 1) : 0u;
+                    v[k] = (uint32_t)((((uint64_t)hi_w << 32) | lo_w) >> sh) & mask;
+                }
+            }
+            if (deltas) {       // ids = prefix sums of the gaps, from 0 in every segment
+                v[1] += v[0];
+                v[2] += v[1];
+                v[3] += v[2];
+                const uint32_t incl = warp_incl_scan(v[3]);
+                const uint32_t pre = incl - v[3];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) v[k] += pre;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (v[k] >= lo && v[k] < hi) visit(v[k], inc);
         }
     }
 }
@@ -959,6 +1060,10 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
 
     const int list = SMALL ? kListDenseSmall : kListDenseWide;
     const uint32_t P_list = (uint32_t)dense_parts(ix, W, T, SMALL);
+    // the tile directory of this counter width, when built for this tile size
+    const uint32_t *dir = SMALL ? ix.dir8 : ix.dir32;
+    const bool use_dir = dir != nullptr && ix.dir_slot != nullptr && W.unit_key != nullptr &&
+                         (SMALL ? ix.dir8_tile : ix.dir32_tile) == (int32_t)tile_cap;
     for (;;) {
         if (tid == 0) {
             uint2 wk;
@@ -979,11 +1084,15 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
         const bool single = qi.n_units <= kItemChunk;
         const bool weighted = (qi.flags & kFlagWeighted) != 0;
         if (tid == 0) s_nS = 0;
-        // cursor of every item at the part's first id
+        // per unit of a single-chunk query: its tile-directory row, kept in
+        // cur as -1 - row, or else a cursor at the part's first id
         if (single && (int32_t)tid < qi.n_units) {
             const int64_t it = qi.unit0 + tid;
             const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
-            cur[tid] = (t0 == 0 || e0 == s0) ? s0 : first_unit_near(ix, s0, e0, (uint32_t)(t0 * tile_cap), N);
+            const uint32_t row = (use_dir && e0 > s0) ? ix.dir_slot[W.unit_key[it]] : 0xFFFFFFFFu;
+            cur[tid] = row != 0xFFFFFFFFu ? -1 - (int64_t)row
+                                          : ((t0 == 0 || e0 == s0) ? s0
+                                                                   : first_unit_near(ix, s0, e0, (uint32_t)(t0 * tile_cap), N));
         }
         __syncthreads();
         for (uint64_t t = t0; t < t1; ++t) {
@@ -1002,17 +1111,33 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                 if ((int32_t)tid < mc) {
                     const int64_t it = qi.unit0 + c0 + tid;
                     const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
-                    int64_t a = single ? cur[tid] : (t == 0 ? s0 : first_unit(ix, s0, e0, tile_lo));
-                    int64_t b = (tile_hi >= N) ? e0 : next_unit_near(ix, a, s0, e0, tile_lo, tile_hi, N);
+                    uint32_t row = 0xFFFFFFFFu;
+                    if (single) {
+                        if (cur[tid] < 0) row = (uint32_t)(-1 - cur[tid]);
+                    } else if (use_dir && e0 > s0) {
+                        row = ix.dir_slot[W.unit_key[it]];
+                    }
+                    int64_t a, b;
+                    if (row != 0xFFFFFFFFu) {
+                        // the tile's cut from the directory: the first id (segment) at or past
+                        // each bound; a compressed segment straddling tile_lo starts the cut
+                        const uint32_t *r = dir + (size_t)row * (size_t)(ntiles + 1);
+                        const uint32_t fa = __ldg(r + t), fb = __ldg(r + t + 1);
+                        a = s0 + (ix.codec ? (fa ? fa - 1 : 0) : fa);
+                        b = s0 + fb;
+                    } else {
+                        a = single ? cur[tid] : (t == 0 ? s0 : first_unit(ix, s0, e0, tile_lo));
+                        b = (tile_hi >= N) ? e0 : next_unit_near(ix, a, s0, e0, tile_lo, tile_hi, N);
+                        // a compressed segment may straddle tile_hi: the next tile starts at it again
+                        if (single) cur[tid] = (ix.codec && b > a) ? b - 1 : b;
+                    }
                     st.start[tid] = a;
                     st.inc[tid] = W.inc[it];
                     len = (uint32_t)(b - a);
                     st.len[tid] = len;
-                    // a compressed segment may straddle tile_hi: the next tile starts at it again
-                    if (single) cur[tid] = (ix.codec && b > a) ? b - 1 : b;
                 }
-                // plain lists go by warp tasks of kRun positions; segments one per warp
-                const uint32_t units = ix.codec ? len : (len + kRun - 1) / kRun;
+                // plain lists go by warp tasks of kRun positions, segments in runs of kSegRun
+                const uint32_t units = ix.codec ? (len + kSegRun - 1) / kSegRun : (len + kRun - 1) / kRun;
                 uint32_t tot = 0;
                 uint32_t off = block_excl_scan(units, ss.tmp, &tot);
                 if ((int32_t)tid < mc) st.flat[tid] = off;
@@ -1026,13 +1151,13 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                         if (GG_OK(loc, n_ids, 3))
                             atomicAdd((uint32_t *)((unsigned char *)cnt + (loc & ~3u)), __funnelshift_l(0u, 1u, loc << 3));
                     };
-                    if (ix.codec) stream_segments(ix, st, (uint32_t)mc, tot, tile_lo, tile_hi, add);
+                    if (ix.codec) stream_segment_runs(ix, st, (uint32_t)mc, tot, tile_lo, tile_hi, add);
                     else stream_runs(ix.ids, st, (uint32_t)mc, tot, add);
                 } else {
                     auto add = [&](uint32_t id, uint32_t inc) {
                         if (GG_OK(id - tile_lo, n_ids, 3)) atomicAdd(&cnt[id - tile_lo], inc);
                     };
-                    if (ix.codec) stream_segments(ix, st, (uint32_t)mc, tot, tile_lo, tile_hi, add);
+                    if (ix.codec) stream_segment_runs(ix, st, (uint32_t)mc, tot, tile_lo, tile_hi, add);
                     else stream_runs(ix.ids, st, (uint32_t)mc, tot, add);
                 }
                 __syncthreads();

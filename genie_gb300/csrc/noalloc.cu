@@ -120,6 +120,7 @@ extern "C" int genie_search_noalloc(genie_index *ix, const genie_queries *q, con
     w.span_start = (int64_t *)(base + kNa.span_start);
     w.span_len = (int64_t *)(base + kNa.span_len);
     w.inc = (uint32_t *)(base + kNa.inc);
+    w.unit_key = nullptr;         // no tile directories: lists are searched per tile
     w.qinfo = (QInfo *)(base + kNa.qinfo);
     w.work = (uint2 *)(base + kNa.work);
     w.work_stride = kNaMaxQueries * kMaxParts;

@@ -1,0 +1,127 @@
+// tile_dir.cu -- tile directories of a resident index.
+//
+// The dense kernel counts a query one id tile at a time, so for every tile it
+// needs, in each posting list the query covers, the positions where the tile
+// begins and ends.  Searching for them (chains of dependent global loads per
+// list per tile, while the rest of the block waits) took a quarter of the
+// dense kernel's time on the uneven-range batch.  A tile directory holds, for
+// every long list and every tile boundary t * tile, the offset in the list of
+// the first id >= t * tile (for a compressed list: of the first segment
+// starting at >= t * tile); a tile's cut of a list is then two independent
+// loads.
+//
+// Layout: dir_slot[key] is the row of a key (~0u: no row, the list is short
+// and is searched), row r holds ntiles + 1 u32 offsets relative to the list
+// start.  Rows are shared by the directories of the two counter widths (one
+// per tile size).  A directory is built once per (index, tile size) by one
+// thread per (row, boundary) and kept while the index lives: batches capture
+// its address in their CUDA graphs.
+#include "capi_internal.h"
+
+#include <algorithm>
+
+namespace gg {
+namespace {
+
+constexpr int64_t kDirMinIds = 256;              // lists this long get a row (plain index)
+constexpr int64_t kDirMinSegs = 4;               // segments, for a compressed index
+constexpr size_t kDirBudget = size_t(1) << 30;   // bytes of one directory at most
+
+__global__ void k_tile_dir(const uint32_t *__restrict__ keys_first, const int64_t *__restrict__ list_off,
+                           const uint32_t *__restrict__ row_key, int64_t n_rows, int64_t ntiles, int64_t tile,
+                           uint32_t *__restrict__ dir) {
+    const int64_t n = n_rows * (ntiles + 1);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / (ntiles + 1), t = i - r * (ntiles + 1);
+        const uint32_t key = row_key[r];
+        const int64_t a = list_off[key], e = list_off[key + 1];
+        const uint64_t x = (uint64_t)t * (uint64_t)tile;
+        const int64_t pos = (t == ntiles || x > 0xFFFFFFFFull) ? e : lower_bound_u32(keys_first, a, e, (uint32_t)x);
+        dir[i] = (uint32_t)(pos - a);
+    }
+}
+
+// Rows of the index's long lists (once per index); false when it has none.
+bool ensure_dir_rows(genie_index *ix) {
+    if (ix->dir_rows_ready) return ix->dir_rows > 0;
+    ix->dir_rows_ready = true;
+    ix->dir_rows = -1;
+    const int64_t nk = ix->host.n_keys();
+    if (nk <= 0 || nk >= (int64_t)0xFFFFFFFFll) return false;
+    std::vector<int64_t> off;
+    int64_t min_len = kDirMinIds;
+    if (ix->codec) {            // segment offsets of the keys
+        off.resize((size_t)nk + 1);
+        if (cudaMemcpy(off.data(), ix->d_key_seg.p, (size_t)(nk + 1) * 8, cudaMemcpyDeviceToHost)) {
+            cudaGetLastError();
+            return false;
+        }
+        min_len = kDirMinSegs;
+    } else {
+        off = ix->host.key_off;
+    }
+    std::vector<uint32_t> slot((size_t)nk, 0xFFFFFFFFu), row_key;
+    for (int64_t k = 0; k < nk; ++k)
+        if (off[k + 1] - off[k] >= min_len) {
+            slot[(size_t)k] = (uint32_t)row_key.size();
+            row_key.push_back((uint32_t)k);
+        }
+    if (row_key.empty()) return false;
+    cudaError_t e;
+    if ((e = ix->d_dir_slot.reserve(slot.size() * 4)) ||
+        (e = cudaMemcpy(ix->d_dir_slot.p, slot.data(), slot.size() * 4, cudaMemcpyHostToDevice)) ||
+        (e = ix->d_dir_row_key.reserve(row_key.size() * 4)) ||
+        (e = cudaMemcpy(ix->d_dir_row_key.p, row_key.data(), row_key.size() * 4, cudaMemcpyHostToDevice))) {
+        cudaGetLastError();
+        return false;
+    }
+    ix->dir_rows = (int64_t)row_key.size();
+    return true;
+}
+
+// The directory of one tile size (built on first use); nullptr when the index
+// has no long lists or the directory would exceed its budget.
+const uint32_t *tile_dir(genie_index *ix, int32_t tile) {
+    if (tile <= 0) return nullptr;
+    for (const auto &d : ix->dirs)
+        if (d.first == tile) return (const uint32_t *)d.second->p;
+    if (!ensure_dir_rows(ix)) return nullptr;
+    const int64_t ntiles = (ix->host.n_objects + tile - 1) / tile;
+    const size_t bytes = (size_t)ix->dir_rows * (size_t)(ntiles + 1) * 4;
+    if (bytes > kDirBudget) return nullptr;
+    DevBuf *b = new DevBuf();
+    if (b->reserve(bytes)) {
+        cudaGetLastError();
+        delete b;
+        return nullptr;
+    }
+    const uint32_t *first = ix->codec ? ix->dev.seg_first : ix->dev.ids;
+    const int64_t *off = ix->codec ? ix->dev.key_seg : ix->dev.key_off;
+    const int64_t n = ix->dir_rows * (ntiles + 1);
+    const int grid = (int)std::min<int64_t>((n + 255) / 256, 152 * 32);
+    k_tile_dir<<<grid, 256, 0, ix->stream>>>(first, off, (const uint32_t *)ix->d_dir_row_key.p, ix->dir_rows,
+                                             ntiles, tile, (uint32_t *)b->p);
+    if (cudaGetLastError() || cudaStreamSynchronize(ix->stream)) {
+        cudaGetLastError();
+        b->release();
+        delete b;
+        return nullptr;
+    }
+    ix->dirs.emplace_back(tile, b);
+    return (const uint32_t *)b->p;
+}
+
+}  // namespace
+
+DevIndex index_view(genie_index *ix, const Tuning &t) {
+    std::lock_guard<std::mutex> g(ix->dir_mu);
+    DevIndex d = ix->dev;
+    d.dir8 = tile_dir(ix, t.dense_tile_u8);
+    d.dir32 = tile_dir(ix, t.dense_tile_u32);
+    d.dir8_tile = d.dir8 ? t.dense_tile_u8 : 0;
+    d.dir32_tile = d.dir32 ? t.dense_tile_u32 : 0;
+    d.dir_slot = (d.dir8 || d.dir32) ? (const uint32_t *)ix->d_dir_slot.p : nullptr;
+    return d;
+}
+
+}  // namespace gg

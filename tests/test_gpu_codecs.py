@@ -95,3 +95,19 @@ def test_compressed_short_segments_and_batch(genie, oracle):
         t2 = genie.Table.load(p)
         ids2, cnt2 = genie.search(t2, qb)
         assert np.array_equal(ids2, oid) and np.array_equal(cnt2, ocnt)
+
+
+@pytest.mark.parametrize("codec", [3, 11, 12, 13])
+def test_bp32_block_segments_dense_exact(genie, oracle, codec):
+    """Full 128-id segments of the BP32-based codecs are unpacked by the dense
+    kernel's word-level path (list tails by the generic decoder): every query
+    forced onto the dense kernel, weighted and not, equals the oracle."""
+    values, batch = _zipf_table(300_000, 8, 1500, 90 + codec)
+    t = genie.Table.compressed(values, codec, 128)
+    qb = genie.QueryBatch(batch["item_off"], batch["dim"], batch["low"], batch["up"], batch["k"],
+                          batch["weight"], batch["weighted"])
+    bt = genie.Batch(t, qb.n_queries, len(batch["dim"]), 300, use_graph=False)
+    bt.set_tuning(sparse_max_total=1, bitmap_bits=-1)
+    ids, cnt, sc = bt.run(qb, scores=True)
+    oid, ocnt, osc, _ = oracle.Index(values).search(qb.as_oracle_batch())
+    assert np.array_equal(cnt, ocnt) and np.array_equal(ids, oid) and np.array_equal(sc, osc)
