@@ -32,7 +32,7 @@ class GenieBatchConfig(ctypes.Structure):
 class GenieTuning(ctypes.Structure):
     _fields_ = [("sparse_slots", I32), ("sparse_ctas_per_sm", I32), ("dense_tile", I32),
                 ("dense_threads", I32), ("sparse_max_total", I64), ("dense_part_work", I64),
-                ("sparse_load_pct", I32), ("bitmap_bits", I32)]
+                ("sparse_load_pct", I32), ("bitmap_bits", I32), ("dense_bitmaps", I32)]
 
 
 class GenieServerConfig(ctypes.Structure):

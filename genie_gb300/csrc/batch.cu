@@ -199,6 +199,8 @@ Tuning from_public(const Tuning &base, const genie_tuning &t) {
     if (t.dense_part_work > 0) r.dense_part_work = t.dense_part_work;
     if (t.bitmap_bits > 0) r.bitmap_bits = t.bitmap_bits;
     if (t.bitmap_bits < 0) r.bitmap_bits = 0;
+    if (t.dense_bitmaps > 0) r.dense_bitmaps = t.dense_bitmaps & 3;
+    if (t.dense_bitmaps < 0) r.dense_bitmaps = 0;
     return r;
 }
 
@@ -211,6 +213,7 @@ void to_public(const Tuning &r, genie_tuning &t) {
     t.dense_part_work = r.dense_part_work;
     t.sparse_load_pct = r.sparse_load_pct;
     t.bitmap_bits = r.bitmap_bits > 0 ? r.bitmap_bits : -1;
+    t.dense_bitmaps = r.dense_bitmaps > 0 ? r.dense_bitmaps : -1;
 }
 
 }  // namespace

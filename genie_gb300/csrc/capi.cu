@@ -340,6 +340,8 @@ genie_index::~genie_index() {
     ws.release();
     d_dir_slot.release();
     d_dir_row_key.release();
+    d_bm_slot.release();
+    d_bm_rows.release();
     for (auto &d : dirs) {
         d.second->release();
         delete d.second;

@@ -100,6 +100,9 @@ struct genie_index {
     bool dir_rows_ready = false;
     int64_t dir_rows = -1;
     gg::DevBuf d_dir_slot, d_dir_row_key;
+    bool bm_ready = false;
+    int64_t bm_words = 0;
+    gg::DevBuf d_bm_slot, d_bm_rows;
     std::vector<std::pair<int32_t, gg::DevBuf *>> dirs;
     cudaStream_t stream = nullptr;
     std::mutex mu;                   // serialises searches on this handle's workspace

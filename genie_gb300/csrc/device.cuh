@@ -63,6 +63,12 @@ struct DevIndex {
     const uint32_t *dir32;
     int32_t dir8_tile;
     int32_t dir32_tile;
+    // presence bitmaps of the dense lists (tile_dir.cu): bm_slot[key] = row of
+    // a list holding >= 1/16 of the objects (~0u: none); a row is bm_words
+    // words, bit o set when object o is listed.  Null when absent.
+    const uint32_t *bm_slot;
+    const uint32_t *bm_rows;
+    int64_t bm_words;
 };
 
 struct DevQueries {
@@ -112,6 +118,7 @@ struct Tuning {
     int32_t bitmap_multi_slots;    // slots of its table of ids seen twice or more
     int32_t bitmap_ready;          // 1 when its shared memory fits the id space (set per launch)
     int32_t num_sms;               // SMs of the device (set per launch)
+    int32_t dense_bitmaps;         // counter widths whose dense lists use their bitmaps: 1 bytes, 2 words
 };
 
 // Work lists, one per kernel variant.

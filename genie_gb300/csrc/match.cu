@@ -1056,7 +1056,12 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
     st.inc = (uint32_t *)(it_raw + kItemChunk * 20);
     st.flat = (uint32_t *)(it_raw + kItemChunk * 24);
     SelectScratch &ss = *(SelectScratch *)(it_raw + kItemChunk * 28 + 16);
-    __shared__ uint32_t s_q, s_p, s_nS, s_nc, s_L;
+    // units counted from a dense-list bitmap: their bitmap row and increment,
+    // and per unit of a single-chunk query its bitmap row (~0u: none)
+    uint32_t *bm_row = (uint32_t *)(it_raw + kItemChunk * 28 + 16 + sizeof(SelectScratch));
+    uint32_t *bm_inc = bm_row + kItemChunk;
+    uint32_t *unit_bm = bm_inc + kItemChunk;
+    __shared__ uint32_t s_q, s_p, s_nS, s_nc, s_L, s_nbm;
 
     const int list = SMALL ? kListDenseSmall : kListDenseWide;
     const uint32_t P_list = (uint32_t)dense_parts(ix, W, T, SMALL);
@@ -1064,6 +1069,9 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
     const uint32_t *dir = SMALL ? ix.dir8 : ix.dir32;
     const bool use_dir = dir != nullptr && ix.dir_slot != nullptr && W.unit_key != nullptr &&
                          (SMALL ? ix.dir8_tile : ix.dir32_tile) == (int32_t)tile_cap;
+    // dense lists counted from their bitmaps (tiles start at a word boundary)
+    const bool use_bm = ix.bm_slot != nullptr && W.unit_key != nullptr && tile_cap % 32u == 0 &&
+                        (T.dense_bitmaps & (SMALL ? 1 : 2)) != 0;
     for (;;) {
         if (tid == 0) {
             uint2 wk;
@@ -1083,12 +1091,17 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
         const uint64_t t0 = ntiles * p / P, t1 = ntiles * (p + 1) / P;
         const bool single = qi.n_units <= kItemChunk;
         const bool weighted = (qi.flags & kFlagWeighted) != 0;
-        if (tid == 0) s_nS = 0;
+        if (tid == 0) {
+            s_nS = 0;
+            s_nbm = 0;
+        }
         // per unit of a single-chunk query: its tile-directory row, kept in
-        // cur as -1 - row, or else a cursor at the part's first id
+        // cur as -1 - row, or else a cursor at the part's first id; and its
+        // dense-list bitmap row
         if (single && (int32_t)tid < qi.n_units) {
             const int64_t it = qi.unit0 + tid;
             const int64_t s0 = W.span_start[it], e0 = s0 + W.span_len[it];
+            unit_bm[tid] = (use_bm && e0 > s0) ? ix.bm_slot[W.unit_key[it]] : 0xFFFFFFFFu;
             const uint32_t row = (use_dir && e0 > s0) ? ix.dir_slot[W.unit_key[it]] : 0xFFFFFFFFu;
             cur[tid] = row != 0xFFFFFFFFu ? -1 - (int64_t)row
                                           : ((t0 == 0 || e0 == s0) ? s0
@@ -1118,7 +1131,14 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                         row = ix.dir_slot[W.unit_key[it]];
                     }
                     int64_t a, b;
-                    if (row != 0xFFFFFFFFu) {
+                    const uint32_t brow = single ? unit_bm[tid]
+                                                 : ((use_bm && e0 > s0) ? ix.bm_slot[W.unit_key[it]] : 0xFFFFFFFFu);
+                    if (brow != 0xFFFFFFFFu) {          // counted from its bitmap, not streamed
+                        const uint32_t at = atomicAdd(&s_nbm, 1u);
+                        bm_row[at] = brow;
+                        bm_inc[at] = W.inc[it];
+                        a = b = s0;
+                    } else if (row != 0xFFFFFFFFu) {
                         // the tile's cut from the directory: the first id (segment) at or past
                         // each bound; a compressed segment straddling tile_lo starts the cut
                         const uint32_t *r = dir + (size_t)row * (size_t)(ntiles + 1);
@@ -1144,6 +1164,47 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                 if (tid == 0) st.flat[mc] = tot;
                 __syncthreads();
                 if (tot) any_ids = true;
+                // dense lists from their bitmaps: thread j owns the tile's objects
+                // 32j .. 32j+31 (counter words 8j .. 8j+7, or 32j .. 32j+31), so the
+                // adds need no atomics; the id stream below waits for them
+                const uint32_t nbm = s_nbm;
+                if (nbm) {
+                    any_ids = true;
+                    const uint32_t *rows = ix.bm_rows + (tile_lo >> 5);
+                    const uint32_t nwords = (n_ids + 31) >> 5;
+                    constexpr uint32_t kBmLoads = 8;      // bitmap words in flight per thread
+                    for (uint32_t j = tid; j < nwords; j += blockDim.x) {
+                        for (uint32_t u0 = 0; u0 < nbm; u0 += kBmLoads) {
+                            uint32_t w[kBmLoads];
+#pragma unroll
+                            for (uint32_t i = 0; i < kBmLoads; ++i)
+                                w[i] = u0 + i < nbm ? __ldg(rows + (size_t)bm_row[u0 + i] * (size_t)ix.bm_words + j) : 0u;
+                            if (SMALL) {
+                                uint32_t acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+                                for (uint32_t i = 0; i < kBmLoads; ++i)
+#pragma unroll
+                                    for (int k = 0; k < 8; ++k)  // four bits -> four byte counters
+                                        acc[k] += (((w[i] >> (4 * k)) & 15u) * 0x00204081u) & 0x01010101u;
+#pragma unroll
+                                for (int k = 0; k < 8; ++k) cnt[8 * j + k] += acc[k];
+                            } else {
+#pragma unroll
+                                for (uint32_t i = 0; i < kBmLoads; ++i) {
+                                    const uint32_t inc = u0 + i < nbm ? bm_inc[u0 + i] : 0u;
+                                    uint32_t x = w[i];
+                                    while (x) {
+                                        const uint32_t bit = (uint32_t)__ffs((int)x) - 1u;
+                                        cnt[32 * j + bit] += inc;
+                                        x &= x - 1u;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    __syncthreads();
+                    if (tid == 0) s_nbm = 0;
+                }
                 if (SMALL) {
                     // byte counters, four to a word: the word at loc & ~3, the byte (loc & 3)
                     auto add = [&](uint32_t id, uint32_t) {
@@ -1259,7 +1320,8 @@ size_t sparse_smem_bytes(const Tuning &t, bool packed) {
 
 size_t dense_smem_bytes(const Tuning &t, bool small) {
     size_t c = (size_t)(small ? t.dense_tile_u8 : t.dense_tile_u32 * 4);
-    return c + (size_t)kMaxK * 8 + (size_t)kCandCap * 8 + kItemChunk * 28 + 16 + sizeof(SelectScratch) + 64;
+    return c + (size_t)kMaxK * 8 + (size_t)kCandCap * 8 + kItemChunk * 28 + 16 + sizeof(SelectScratch) + kItemChunk * 12 +
+           64;
 }
 
 Tuning default_tuning() {
@@ -1278,6 +1340,7 @@ Tuning default_tuning() {
     t.bitmap_bits = 1179648;         // id spaces up to 144 KiB of presence bits
     t.bitmap_multi_slots = 2048;     // 8 KiB table of repeated ids
     t.bitmap_ready = 0;              // set per launch
+    t.dense_bitmaps = 3;             // dense lists from their bitmaps for both counter widths
     return t;
 }
 

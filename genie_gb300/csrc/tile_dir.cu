@@ -1,4 +1,4 @@
-// tile_dir.cu -- tile directories of a resident index.
+// tile_dir.cu -- tile directories and dense-list bitmaps of a resident index.
 //
 // The dense kernel counts a query one id tile at a time, so for every tile it
 // needs, in each posting list the query covers, the positions where the tile
@@ -16,7 +16,18 @@
 // per tile size).  A directory is built once per (index, tile size) by one
 // thread per (row, boundary) and kept while the index lives: batches capture
 // its address in their CUDA graphs.
+//
+// Dense-list bitmaps: a posting list holding at least 1/16 of the objects
+// (the lists of a dimension's most common value) is also kept as a presence
+// bitmap of n_objects bits, a tenth or less of its ids' bytes at such
+// densities.  The dense kernel counts such a list from its bitmap words
+// (each thread owns 32 objects of the tile, so plain adds replace the
+// shared-memory atomics) and streams (or decodes) only the other lists.
+// Built once per index with one value per object and dim (no list repeats an
+// id; a compressed index decodes its dense lists' segments to build them), on
+// first use, within a budget; kept while the index lives.
 #include "capi_internal.h"
+#include "codecs.cuh"
 
 #include <algorithm>
 
@@ -26,6 +37,22 @@ namespace {
 constexpr int64_t kDirMinIds = 256;              // lists this long get a row (plain index)
 constexpr int64_t kDirMinSegs = 4;               // segments, for a compressed index
 constexpr size_t kDirBudget = size_t(1) << 30;   // bytes of one directory at most
+constexpr int64_t kBmMinObjects = 65536;         // id spaces too small for bitmaps to pay
+constexpr int64_t kBmDensity = 16;               // a list with len * 16 >= n_objects gets a bitmap
+constexpr size_t kBmBudget = size_t(2) << 30;    // bytes of all bitmap rows at most
+
+// Bit o of row r for every id o of row r's list; one CTA row per blockIdx.y.
+__global__ void k_bm_build(const uint32_t *__restrict__ ids, const int64_t *__restrict__ key_off,
+                           const uint32_t *__restrict__ row_key, int64_t words, uint32_t *__restrict__ rows) {
+    const uint32_t r = blockIdx.y;
+    const uint32_t key = row_key[r];
+    const int64_t a = key_off[key], e = key_off[key + 1];
+    uint32_t *row = rows + (size_t)r * (size_t)words;
+    for (int64_t p = a + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < e; p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t id = ids[p];
+        atomicOr(&row[id >> 5], 1u << (id & 31u));
+    }
+}
 
 __global__ void k_tile_dir(const uint32_t *__restrict__ keys_first, const int64_t *__restrict__ list_off,
                            const uint32_t *__restrict__ row_key, int64_t n_rows, int64_t ntiles, int64_t tile,
@@ -111,6 +138,75 @@ const uint32_t *tile_dir(genie_index *ix, int32_t tile) {
     return (const uint32_t *)b->p;
 }
 
+// The same for a compressed index: warp w of the block decodes segments
+// w, w + warps, ... of row r's list and sets their ids' bits.
+__global__ void k_bm_build_compressed(int codec, const uint32_t *__restrict__ words,
+                                      const int64_t *__restrict__ seg_word_off, const int64_t *__restrict__ key_seg,
+                                      const uint32_t *__restrict__ row_key, int64_t n_words_row,
+                                      uint32_t *__restrict__ rows) {
+    const uint32_t r = blockIdx.y;
+    const uint32_t key = row_key[r];
+    uint32_t *row = rows + (size_t)r * (size_t)n_words_row;
+    const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t w0 = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    for (int64_t sg = key_seg[key] + w0; sg < key_seg[key + 1]; sg += warps) {
+        auto set = [&](uint32_t id, uint32_t) { atomicOr(&row[id >> 5], 1u << (id & 31u)); };
+        decode_segment_values(codec, words, seg_word_off[sg], seg_word_off[sg + 1], set);
+    }
+}
+
+// The dense-list bitmaps (built on first use); false when the index has none.
+bool dense_bitmaps(genie_index *ix) {
+    if (ix->bm_ready) return ix->bm_words > 0;
+    ix->bm_ready = true;
+    ix->bm_words = 0;
+    const int64_t n = ix->host.n_objects, nk = ix->host.n_keys();
+    if (ix->is_bag || ix->sub_shift >= 0 || n < kBmMinObjects || nk <= 0 ||
+        nk >= (int64_t)0xFFFFFFFFll)
+        return false;
+    const int64_t words = (n + 31) / 32;
+    std::vector<uint32_t> slot((size_t)nk, 0xFFFFFFFFu), row_key;
+    for (int64_t k = 0; k < nk; ++k)
+        if ((ix->host.key_off[k + 1] - ix->host.key_off[k]) * kBmDensity >= n &&
+            (row_key.size() + 1) * (size_t)words * 4 <= kBmBudget && row_key.size() < 65535) {
+            slot[(size_t)k] = (uint32_t)row_key.size();
+            row_key.push_back((uint32_t)k);
+        }
+    if (row_key.empty()) return false;
+    DevBuf rk;
+    cudaError_t e;
+    if ((e = ix->d_bm_slot.reserve(slot.size() * 4)) ||
+        (e = cudaMemcpy(ix->d_bm_slot.p, slot.data(), slot.size() * 4, cudaMemcpyHostToDevice)) ||
+        (e = rk.reserve(row_key.size() * 4)) ||
+        (e = cudaMemcpy(rk.p, row_key.data(), row_key.size() * 4, cudaMemcpyHostToDevice)) ||
+        (e = ix->d_bm_rows.reserve(row_key.size() * (size_t)words * 4)) ||
+        (e = cudaMemsetAsync(ix->d_bm_rows.p, 0, row_key.size() * (size_t)words * 4, ix->stream))) {
+        cudaGetLastError();
+        rk.release();
+        ix->d_bm_slot.release();
+        ix->d_bm_rows.release();
+        return false;
+    }
+    if (ix->codec)
+        k_bm_build_compressed<<<dim3(64, (unsigned)row_key.size()), 256, 0, ix->stream>>>(
+            ix->codec, ix->dev.words, ix->dev.seg_word_off, ix->dev.key_seg, (const uint32_t *)rk.p, words,
+            (uint32_t *)ix->d_bm_rows.p);
+    else
+        k_bm_build<<<dim3(64, (unsigned)row_key.size()), 256, 0, ix->stream>>>(
+            ix->dev.ids, ix->dev.key_off, (const uint32_t *)rk.p, words, (uint32_t *)ix->d_bm_rows.p);
+    e = cudaGetLastError();
+    if (!e) e = cudaStreamSynchronize(ix->stream);
+    rk.release();
+    if (e) {
+        cudaGetLastError();
+        ix->d_bm_slot.release();
+        ix->d_bm_rows.release();
+        return false;
+    }
+    ix->bm_words = words;
+    return true;
+}
+
 }  // namespace
 
 DevIndex index_view(genie_index *ix, const Tuning &t) {
@@ -121,6 +217,10 @@ DevIndex index_view(genie_index *ix, const Tuning &t) {
     d.dir8_tile = d.dir8 ? t.dense_tile_u8 : 0;
     d.dir32_tile = d.dir32 ? t.dense_tile_u32 : 0;
     d.dir_slot = (d.dir8 || d.dir32) ? (const uint32_t *)ix->d_dir_slot.p : nullptr;
+    const bool bm = dense_bitmaps(ix);
+    d.bm_slot = bm ? (const uint32_t *)ix->d_bm_slot.p : nullptr;
+    d.bm_rows = bm ? (const uint32_t *)ix->d_bm_rows.p : nullptr;
+    d.bm_words = bm ? ix->bm_words : 0;
     return d;
 }
 

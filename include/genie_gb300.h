@@ -252,6 +252,8 @@ typedef struct {
     int64_t dense_part_work;    /* posting ids per dense id-range part */
     int32_t sparse_load_pct;    /* posting ids per part <= this % of the hash slots */
     int32_t bitmap_bits;        /* largest id space (objects) of the bitmap kernel; -1: off */
+    int32_t dense_bitmaps;      /* dense lists counted from their presence bitmaps: 1 for unweighted
+                                   queries, 2 for weighted ones, 3 both, -1 never */
 } genie_tuning;
 
 /* Batched search over one resident index: fixed-capacity device buffers,
