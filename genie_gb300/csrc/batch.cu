@@ -363,16 +363,19 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
     if (rc) return rc;
     const Tuning base = b->tuning;
     // hash slots, CTAs per SM (2: 512 threads, 1: 1024 threads), load %, dense tile,
-    // crossover, largest id space of the bitmap kernel (-1: bitmap kernel off)
-    struct Cand { int32_t slots, ctas, load, tile; int64_t smax; int32_t bits; };
+    // crossover, largest id space of the bitmap kernel (-1: bitmap kernel off),
+    // counter widths whose dense lists use their bitmaps (-1: none)
+    struct Cand { int32_t slots, ctas, load, tile; int64_t smax; int32_t bits, dbm; };
     const Cand cands[] = {
-        {22528, 2, 50, 147456, 270336, -1}, {11264, 2, 50, 147456, 270336, -1},
-        {22528, 2, 60, 147456, 270336, -1}, {45056, 1, 50, 147456, 270336, -1},
-        {53248, 1, 56, 147456, 270336, -1}, {53248, 1, 62, 147456, 270336, -1},
-        {22528, 2, 50, 98304, 270336, -1},  {22528, 2, 50, 147456, 67584, -1},
-        {53248, 1, 62, 147456, 1081344, -1},
-        {53248, 1, 56, 147456, 270336, 1179648}, {53248, 1, 56, 147456, 1081344, 1179648},
-        {22528, 2, 50, 147456, 270336, 1179648},
+        {22528, 2, 50, 147456, 270336, -1, 1}, {11264, 2, 50, 147456, 270336, -1, 1},
+        {22528, 2, 60, 147456, 270336, -1, 1}, {45056, 1, 50, 147456, 270336, -1, 1},
+        {53248, 1, 56, 147456, 270336, -1, 1}, {53248, 1, 62, 147456, 270336, -1, 1},
+        {22528, 2, 50, 98304, 270336, -1, 1},  {22528, 2, 50, 147456, 67584, -1, 1},
+        {53248, 1, 62, 147456, 1081344, -1, 1},
+        {53248, 1, 56, 147456, 270336, 1179648, 1}, {53248, 1, 56, 147456, 1081344, 1179648, 1},
+        {22528, 2, 50, 147456, 270336, 1179648, 1},
+        {22528, 2, 50, 172032, 270336, -1, 1}, {22528, 2, 50, 147456, 270336, -1, -1},
+        {22528, 2, 50, 172032, 270336, -1, -1},
     };
     float best_ms = 1e30f;
     Tuning best = base;
@@ -384,6 +387,7 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
         t.dense_tile = c.tile;
         t.sparse_max_total = c.smax;
         t.bitmap_bits = c.bits;
+        t.dense_bitmaps = c.dbm;
         if (genie_batch_set_tuning(b, &t)) continue;
         float total = 0.0f;
         bool ok = true;

@@ -1340,7 +1340,7 @@ Tuning default_tuning() {
     t.bitmap_bits = 1179648;         // id spaces up to 144 KiB of presence bits
     t.bitmap_multi_slots = 2048;     // 8 KiB table of repeated ids
     t.bitmap_ready = 0;              // set per launch
-    t.dense_bitmaps = 3;             // dense lists from their bitmaps for both counter widths
+    t.dense_bitmaps = 1;             // dense lists from their bitmaps for byte counters (unweighted)
     return t;
 }
 
