@@ -1174,20 +1174,41 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                     const uint32_t nwords = (n_ids + 31) >> 5;
                     constexpr uint32_t kBmLoads = 8;      // bitmap words in flight per thread
                     for (uint32_t j = tid; j < nwords; j += blockDim.x) {
+                        // byte counters: the lists' bits are summed bit-sliced (plane t holds
+                        // bit t of each object's count so far, at most 24 lists a pass), then
+                        // each nibble of the planes is spread into its four counter bytes
+                        uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, in_pass = 0;
                         for (uint32_t u0 = 0; u0 < nbm; u0 += kBmLoads) {
                             uint32_t w[kBmLoads];
 #pragma unroll
                             for (uint32_t i = 0; i < kBmLoads; ++i)
                                 w[i] = u0 + i < nbm ? __ldg(rows + (size_t)bm_row[u0 + i] * (size_t)ix.bm_words + j) : 0u;
                             if (SMALL) {
-                                uint32_t acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
-                                for (uint32_t i = 0; i < kBmLoads; ++i)
+                                for (uint32_t i = 0; i < kBmLoads; ++i) {     // ripple-carry add of one bit per object
+                                    const uint32_t c0 = p0 & w[i];
+                                    p0 ^= w[i];
+                                    const uint32_t c1 = p1 & c0;
+                                    p1 ^= c0;
+                                    const uint32_t c2 = p2 & c1;
+                                    p2 ^= c1;
+                                    const uint32_t c3 = p3 & c2;
+                                    p3 ^= c2;
+                                    p4 ^= c3;
+                                }
+                                in_pass += kBmLoads;
+                                if (in_pass + kBmLoads > 31 || u0 + kBmLoads >= nbm) {
 #pragma unroll
-                                    for (int k = 0; k < 8; ++k)  // four bits -> four byte counters
-                                        acc[k] += (((w[i] >> (4 * k)) & 15u) * 0x00204081u) & 0x01010101u;
-#pragma unroll
-                                for (int k = 0; k < 8; ++k) cnt[8 * j + k] += acc[k];
+                                    for (int k = 0; k < 8; ++k) {
+                                        auto spread = [](uint32_t x) { return (x * 0x00204081u) & 0x01010101u; };
+                                        const int sh = 4 * k;
+                                        cnt[8 * j + k] += spread((p0 >> sh) & 15u) + (spread((p1 >> sh) & 15u) << 1) +
+                                                          (spread((p2 >> sh) & 15u) << 2) + (spread((p3 >> sh) & 15u) << 3) +
+                                                          (spread((p4 >> sh) & 15u) << 4);
+                                    }
+                                    p0 = p1 = p2 = p3 = p4 = 0;
+                                    in_pass = 0;
+                                }
                             } else {
 #pragma unroll
                                 for (uint32_t i = 0; i < kBmLoads; ++i) {

@@ -10,8 +10,9 @@
 // starting at >= t * tile); a tile's cut of a list is then two independent
 // loads.
 //
-// Layout: dir_slot[key] is the row of a key (~0u: no row, the list is short
-// and is searched), row r holds ntiles + 1 u32 offsets relative to the list
+// Layout: dir_slot[key] is the row of a key (~0u: no row, the list is
+// shorter than the budget allows rows for, and is searched), row r holds
+// ntiles + 1 u32 offsets relative to the list
 // start.  Rows are shared by the directories of the two counter widths (one
 // per tile size).  A directory is built once per (index, tile size) by one
 // thread per (row, boundary) and kept while the index lives: batches capture
@@ -34,9 +35,15 @@
 namespace gg {
 namespace {
 
-constexpr int64_t kDirMinIds = 256;              // lists this long get a row (plain index)
-constexpr int64_t kDirMinSegs = 4;               // segments, for a compressed index
 constexpr size_t kDirBudget = size_t(1) << 30;   // bytes of one directory at most
+// A list shorter than a tile's cut search is worth nothing but still makes
+// the whole block wait for the search: every list gets a row when the
+// directories fit their budget, else lists of at least the smallest of these
+// lengths (ids, or segments of a compressed index) that fits.
+constexpr int64_t kDirMinLens[] = {1, 16, 64, 256, 1024, 4096};
+// the smallest tile a directory is sized for (the 4-byte counter tile of the
+// smallest autotuner tile)
+constexpr int64_t kDirSmallestTile = 98304 / 4;
 constexpr int64_t kBmMinObjects = 65536;         // id spaces too small for bitmaps to pay
 constexpr int64_t kBmDensity = 16;               // a list with len * 16 >= n_objects gets a bitmap
 constexpr size_t kBmBudget = size_t(2) << 30;    // bytes of all bitmap rows at most
@@ -76,16 +83,24 @@ bool ensure_dir_rows(genie_index *ix) {
     const int64_t nk = ix->host.n_keys();
     if (nk <= 0 || nk >= (int64_t)0xFFFFFFFFll) return false;
     std::vector<int64_t> off;
-    int64_t min_len = kDirMinIds;
     if (ix->codec) {            // segment offsets of the keys
         off.resize((size_t)nk + 1);
         if (cudaMemcpy(off.data(), ix->d_key_seg.p, (size_t)(nk + 1) * 8, cudaMemcpyDeviceToHost)) {
             cudaGetLastError();
             return false;
         }
-        min_len = kDirMinSegs;
     } else {
         off = ix->host.key_off;
+    }
+    const int64_t max_tiles = (ix->host.n_objects + kDirSmallestTile - 1) / kDirSmallestTile + 1;
+    int64_t min_len = kDirMinLens[sizeof(kDirMinLens) / sizeof(kDirMinLens[0]) - 1];
+    for (int64_t len : kDirMinLens) {
+        int64_t rows = 0;
+        for (int64_t k = 0; k < nk; ++k) rows += off[k + 1] - off[k] >= len ? 1 : 0;
+        if ((size_t)rows * (size_t)max_tiles * 4 <= kDirBudget) {
+            min_len = len;
+            break;
+        }
     }
     std::vector<uint32_t> slot((size_t)nk, 0xFFFFFFFFu), row_key;
     for (int64_t k = 0; k < nk; ++k)
