@@ -1109,6 +1109,10 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
         }
         __syncthreads();
         for (uint64_t t = t0; t < t1; ++t) {
+            // the query's lower bound, read now so that its latency passes
+            // during the tile's stream (a bound read earlier is still a bound)
+            uint32_t L_early = 0;
+            if (tid == 0) L_early = *(volatile uint32_t *)&W.lb[q];
             const uint32_t tile_lo = (uint32_t)(t * tile_cap);
             const uint32_t tile_hi = (uint32_t)umin64(N, (t + 1) * tile_cap);
             const uint32_t n_ids = tile_hi - tile_lo;
@@ -1251,12 +1255,39 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
             // L, the largest k-th primary a finished tile of another part of
             // the query has found: the query's final k-th primary is at least
             // L, so nothing below it can place.
-            if (tid == 0) s_L = *(volatile uint32_t *)&W.lb[q];
+            if (tid == 0) s_L = L_early;
             __syncthreads();
             const uint32_t nS = s_nS, L = s_L;
             uint32_t thr = nS == qi.k ? key_prim(S[qi.k - 1]) : 0u;
             if (L > 0 && L - 1 > thr) thr = L - 1;
-            if (nS == qi.k || L > 0) {
+            // A query's first tile (nothing known yet), byte counters: T, the
+            // k-th largest of the 16-counter vectors' maxima, bounds the
+            // tile's k-th count from below (k vectors hold a counter >= T),
+            // so the counters >= T hold the tile's top-k.
+            bool bounded = false;
+            if (SMALL && nS == 0 && L == 0) {
+                const uint32_t nvec = (n_ids + 15) / 16;
+                for (uint32_t i = tid; i < 256; i += blockDim.x) ss.hist[i] = 0;
+                __syncthreads();
+                for (uint32_t b = 0; b < nvec; b += blockDim.x) {
+                    const uint32_t v = b + tid;
+                    const bool act = v < nvec;
+                    const uint4 w = act ? ((const uint4 *)cnt)[v] : make_uint4(0, 0, 0, 0);
+                    uint32_t mx = __vmaxu4(__vmaxu4(w.x, w.y), __vmaxu4(w.z, w.w));
+                    mx = __vmaxu4(mx, mx >> 16);
+                    const uint32_t m8 = max(mx & 255u, (mx >> 8) & 255u);
+                    hist_add(ss.hist, m8, act && m8 > 0);
+                }
+                __syncthreads();
+                if (warp_id() == 0) find_digit(ss, qi.k, true);
+                __syncthreads();
+                if (!ss.sc[3]) {
+                    thr = ss.sc[0] - 1;
+                    bounded = true;
+                }
+                __syncthreads();
+            }
+            if (nS == qi.k || L > 0 || bounded) {
                 // Few counters usually pass: collect them behind a copy of S
                 // and sort the union.
                 if (tid == 0) s_nc = 0;
@@ -1266,29 +1297,25 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                 const uint32_t per = SMALL ? 16u : 4u;
                 const uint32_t nvec = (n_ids + per - 1) / per;
                 const uint32_t thr4 = SMALL ? thr * 0x01010101u : thr;
-                for (uint32_t b = 0; b < nvec; b += blockDim.x) {
-                    const uint32_t v = b + tid;
-                    const bool act = v < nvec;
-                    const uint4 w = act ? ((const uint4 *)cnt)[v] : make_uint4(0, 0, 0, 0);
-                    bool any;
-                    if (SMALL)
-                        any = (__vcmpgtu4(w.x, thr4) | __vcmpgtu4(w.y, thr4) | __vcmpgtu4(w.z, thr4) |
-                               __vcmpgtu4(w.w, thr4)) != 0u;
-                    else
-                        any = w.x > thr || w.y > thr || w.z > thr || w.w > thr;
-                    if (__ballot_sync(0xffffffffu, act && any) == 0u) continue;
+                // each thread walks its own passing counters (a handful per
+                // tile), so a vector without one costs a load and compares
+                for (uint32_t v = tid; v < nvec; v += blockDim.x) {
+                    const uint4 w = ((const uint4 *)cnt)[v];
                     const uint32_t words[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-                    for (uint32_t e = 0; e < per; ++e) {
-                        const uint32_t prim = SMALL ? ((words[e >> 2] >> ((e & 3) * 8)) & 255u) : words[e];
-                        const uint32_t local = v * per + e;
-                        const bool keep = act && prim > thr && local < n_ids;
-                        const uint32_t mk = __ballot_sync(0xffffffffu, keep);
-                        if (!mk) continue;
-                        uint32_t at = 0;
-                        if (lane_id() == 0) at = atomicAdd(&s_nc, (uint32_t)__popc(mk));
-                        at = __shfl_sync(0xffffffffu, at, 0) + (uint32_t)__popc(mk & ((1u << lane_id()) - 1u));
-                        if (keep && at < room) cand[nS + at] = make_key(prim, tile_lo + local);
+                    for (uint32_t h = 0; h < 4; ++h) {
+                        // 0xFF in each byte of a passing counter
+                        uint32_t hit = SMALL ? __vcmpgtu4(words[h], thr4) : (words[h] > thr ? 0xFFu : 0u);
+                        while (hit) {
+                            const uint32_t byte = (uint32_t)(__ffs((int)hit) - 1) >> 3;
+                            hit &= ~(0xFFu << (8 * byte));
+                            const uint32_t prim = SMALL ? (words[h] >> (8 * byte)) & 255u : words[h];
+                            const uint32_t local = SMALL ? v * 16 + h * 4 + byte : v * 4 + h;
+                            if (local < n_ids) {
+                                const uint32_t at = atomicAdd(&s_nc, 1u);
+                                if (at < room) cand[nS + at] = make_key(prim, tile_lo + local);
+                            }
+                        }
                     }
                 }
                 __syncthreads();
