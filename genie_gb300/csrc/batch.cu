@@ -405,6 +405,27 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
         }
         b->tuning = base;
     }
+    // then the objects per dense part, in whole tiles of the chosen tile size
+    const Tuning first = best;
+    for (int64_t tiles = 1; tiles <= 4; ++tiles) {
+        b->tuning = first;
+        b->tuning.dense_part_work = tiles * first.dense_tile_u8;
+        b->graph_valid = false;
+        float total = 0.0f;
+        bool ok = true;
+        for (int it = 0; it < 4 && ok; ++it) {
+            if (genie_batch_launch(b, nullptr)) { ok = false; break; }
+            float ms = 0.0f;
+            genie_batch_last_stats(b, nullptr, &ms);
+            if (it > 0) total += ms;
+        }
+        cudaError_t e = cudaStreamSynchronize(b->stream);
+        if (e) return cuda_fail(e, "autotune");
+        if (ok && total < best_ms) {
+            best_ms = total;
+            best = b->tuning;
+        }
+    }
     b->tuning = best;
     b->graph_valid = false;
     if (chosen) to_public(best, *chosen);

@@ -110,7 +110,7 @@ struct Tuning {
     int32_t dense_tile_u32;        // ids per tile, 4-byte counters
     int32_t dense_threads;
     int64_t sparse_max_total;      // more touched ids than this -> dense
-    int64_t dense_part_work;       // touched ids per dense part
+    int64_t dense_part_work;       // objects per dense id-range part (whole tiles, at least one)
     int32_t sparse_ctas_per_sm;
     int32_t dense_ctas_per_sm;
     int32_t sparse_load_pct;       // posting ids per part <= this % of the hash slots

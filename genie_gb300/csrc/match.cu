@@ -41,14 +41,19 @@ void read_oob(unsigned long long out[4]) {
 
 constexpr int kPlanThreads = 256;
 
-// Id-range parts of a dense query: one per counter tile, at most
-// W.max_parts (then a part sweeps several consecutive tiles).  Every dense
-// query of one counter width has the same number, so that the dense kernel
-// can take its work part-major (take_dense).
+// Id-range parts of a dense query: each sweeps T.dense_part_work objects in
+// whole counter tiles (at least one), at most W.max_parts parts.  Fewer,
+// longer parts pay a part's setup and merge less often and let its later
+// tiles merge against a full running top-k.  Every dense query of one
+// counter width has the same number, so that the dense kernel can take its
+// work part-major (take_dense).
 __device__ __forceinline__ int64_t dense_parts(const DevIndex &ix, const Work &W, const Tuning &T, bool small) {
     const int64_t tile = small ? T.dense_tile_u8 : T.dense_tile_u32;
     const int64_t ntiles = (ix.n_objects + tile - 1) / tile;
-    const int64_t pd = ntiles < W.max_parts ? ntiles : W.max_parts;
+    int64_t per = T.dense_part_work / tile;
+    if (per < 1) per = 1;
+    const int64_t np = (ntiles + per - 1) / per;
+    const int64_t pd = np < W.max_parts ? np : W.max_parts;
     return pd < 1 ? 1 : pd;
 }
 
@@ -1381,7 +1386,7 @@ Tuning default_tuning() {
     t.dense_tile_u32 = 36864;        // 144 KiB of 4-byte counters
     t.dense_threads = 1024;
     t.sparse_max_total = 16 * 16896;
-    t.dense_part_work = 4 << 20;
+    t.dense_part_work = 2 * 172032;  // two 172,032-object 1-byte tiles per dense part
     t.sparse_ctas_per_sm = 2;
     t.dense_ctas_per_sm = 1;
     t.sparse_load_pct = 50;

@@ -249,7 +249,7 @@ typedef struct {
     int32_t dense_tile;         /* ids per dense tile (1-byte counters; 4-byte get a quarter) */
     int32_t dense_threads;
     int64_t sparse_max_total;   /* queries touching more posting ids go dense */
-    int64_t dense_part_work;    /* posting ids per dense id-range part */
+    int64_t dense_part_work;    /* objects per dense id-range part, in whole tiles (at least one) */
     int32_t sparse_load_pct;    /* posting ids per part <= this % of the hash slots */
     int32_t bitmap_bits;        /* largest id space (objects) of the bitmap kernel; -1: off */
     int32_t dense_bitmaps;      /* dense lists counted from their presence bitmaps: 1 for unweighted
