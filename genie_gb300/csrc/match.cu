@@ -1182,6 +1182,7 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                     const uint32_t *rows = ix.bm_rows + (tile_lo >> 5);
                     const uint32_t nwords = (n_ids + 31) >> 5;
                     constexpr uint32_t kBmLoads = 8;      // bitmap words in flight per thread
+                    static_assert(kBmLoads == 8, "the adder tree takes eight rows a group");
                     for (uint32_t j = tid; j < nwords; j += blockDim.x) {
                         // byte counters: the lists' bits are summed bit-sliced (plane t holds
                         // bit t of each object's count so far, at most 24 lists a pass), then
@@ -1193,18 +1194,25 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                             for (uint32_t i = 0; i < kBmLoads; ++i)
                                 w[i] = u0 + i < nbm ? __ldg(rows + (size_t)bm_row[u0 + i] * (size_t)ix.bm_words + j) : 0u;
                             if (SMALL) {
-#pragma unroll
-                                for (uint32_t i = 0; i < kBmLoads; ++i) {     // ripple-carry add of one bit per object
-                                    const uint32_t c0 = p0 & w[i];
-                                    p0 ^= w[i];
-                                    const uint32_t c1 = p1 & c0;
-                                    p1 ^= c0;
-                                    const uint32_t c2 = p2 & c1;
-                                    p2 ^= c1;
-                                    const uint32_t c3 = p3 & c2;
-                                    p3 ^= c2;
-                                    p4 ^= c3;
-                                }
+                                // the eight rows' bits into the planes by a carry-save adder
+                                // tree (full adders: sum a^b^c, carry majority(a,b,c)); a group
+                                // adds at most 8, so one weight-8 carry ripples into p3, p4
+                                auto csa = [](uint32_t &s, uint32_t &c, uint32_t a, uint32_t b, uint32_t d) {
+                                    const uint32_t u = a ^ b;
+                                    s = u ^ d;
+                                    c = (a & b) | (u & d);
+                                };
+                                uint32_t t2a, t2b, t2c, t2d, t4a, t4b, t8;
+                                csa(p0, t2a, p0, w[0], w[1]);
+                                csa(p0, t2b, p0, w[2], w[3]);
+                                csa(p1, t4a, p1, t2a, t2b);
+                                csa(p0, t2c, p0, w[4], w[5]);
+                                csa(p0, t2d, p0, w[6], w[7]);
+                                csa(p1, t4b, p1, t2c, t2d);
+                                csa(p2, t8, p2, t4a, t4b);
+                                const uint32_t c3 = p3 & t8;
+                                p3 ^= t8;
+                                p4 ^= c3;
                                 in_pass += kBmLoads;
                                 if (in_pass + kBmLoads > 31 || u0 + kBmLoads >= nbm) {
 #pragma unroll
