@@ -223,10 +223,12 @@ int genie_search_multi(genie_index *const *ix, const genie_queries *q, int32_t n
  * (dim,value) lists covered by queries whose items cover several lists
  * each) and 32768 results per call, larger batches are rejected with
  * GENIE_ERR_INVALID_ARG.  The first call on a device looks up the array's
- * address (and prepares the kernels); make it before any stream capture.
- * Calls are serialised and wait for their device work on `stream` (a
- * cudaStream_t, NULL = legacy default); device work that overlaps a call
- * from elsewhere in the process would race on the shared array. */
+ * address (and prepares the kernels).  Every call is blocking: it
+ * synchronises `stream` (a cudaStream_t, NULL = legacy default) and reads
+ * the device's error word, so no call may be made while any stream is being
+ * captured into a CUDA graph.  Calls are serialised; device work that
+ * overlaps a call from elsewhere in the process would race on the shared
+ * array. */
 int genie_search_noalloc(genie_index *ix, const genie_queries *q, const int64_t *out_off,
                          int64_t n_items, int64_t total_k, uint32_t *out_ids, uint32_t *out_counts,
                          float *out_scores, void *stream);
