@@ -1310,6 +1310,10 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                 const uint32_t per = SMALL ? 16u : 4u;
                 const uint32_t nvec = (n_ids + per - 1) / per;
                 const uint32_t thr4 = SMALL ? thr * 0x01010101u : thr;
+                // bytes above thr < 127: bit 7 of (low seven bits + 127 - thr),
+                // which carries into no other byte, or the byte's own bit 7
+                const bool narrow = SMALL && thr < 127u;
+                const uint32_t bias4 = narrow ? (127u - thr) * 0x01010101u : 0u;
                 // each thread walks its own passing counters (a handful per
                 // tile), so a vector without one costs a load and compares
                 for (uint32_t v = tid; v < nvec; v += blockDim.x) {
@@ -1317,8 +1321,10 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                     const uint32_t words[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
                     for (uint32_t h = 0; h < 4; ++h) {
-                        // 0xFF in each byte of a passing counter
-                        uint32_t hit = SMALL ? __vcmpgtu4(words[h], thr4) : (words[h] > thr ? 0xFFu : 0u);
+                        // a nonzero bit in each byte of a passing counter
+                        uint32_t hit = !SMALL  ? (words[h] > thr ? 0xFFu : 0u)
+                                       : narrow ? ((((words[h] & 0x7F7F7F7Fu) + bias4) | words[h]) & 0x80808080u)
+                                                : __vcmpgtu4(words[h], thr4);
                         while (hit) {
                             const uint32_t byte = (uint32_t)(__ffs((int)hit) - 1) >> 3;
                             hit &= ~(0xFFu << (8 * byte));
