@@ -528,8 +528,13 @@ __device__ __forceinline__ void stream_runs(const uint32_t *__restrict__ ids, co
 // or two words holding its four values of miniblock l/8 (L1 hits after the
 // first lane), extracts them with shifts, and the delta stage is one warp
 // prefix sum.  Other segments (list tails, other codecs) take the generic
-// warp decoder.  Ids outside [lo, hi) are skipped.
-constexpr uint32_t kSegRun = 8;
+// warp decoder.  Ids outside [lo, hi) are skipped.  Runs are one segment
+// long: a tile holds few segments of most lists, so a long run keeps one
+// warp busy while the others wait at the tile's barrier, and the run's
+// per-lane state raises the register pressure of the whole dense kernel
+// (config2 batch: 67.9 ms with runs of 8 segments, 62.4 with 4, 61.3 with 2,
+// 58.3 with 1; spill stores of k_dense 3,740 / 612 / 104 bytes for 8 / 2 / 1).
+constexpr uint32_t kSegRun = 1;
 constexpr uint32_t kBlockIds = 128;
 
 // Whether a codec's full segments are one bare BP32 block (after an optional
