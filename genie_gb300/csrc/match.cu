@@ -486,7 +486,7 @@ constexpr uint32_t kRun = 1024;
 template <class V>
 __device__ __forceinline__ void stream_runs(const uint32_t *__restrict__ ids, const ItemStage &st, uint32_t n_items,
                                             uint32_t n_tasks, V &&visit) {
-    constexpr int R = 16;                 // loads in flight per lane
+    constexpr int R = 32;                 // loads in flight per lane: a full task in one round
     const uint32_t lane = lane_id(), nw = blockDim.x >> 5;
     for (uint32_t f = warp_id(); f < n_tasks; f += nw) {
         uint32_t a = 0, b = n_items;      // last sub-span with flat <= f
