@@ -1193,11 +1193,20 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
                         // bit t of each object's count so far, at most 24 lists a pass), then
                         // each nibble of the planes is spread into its four counter bytes
                         uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0, p4 = 0, in_pass = 0;
+                        // the next group's words load while this group is summed
+                        uint32_t wn[kBmLoads];
+#pragma unroll
+                        for (uint32_t i = 0; i < kBmLoads; ++i)
+                            wn[i] = i < nbm ? __ldg(rows + (size_t)bm_row[i] * (size_t)ix.bm_words + j) : 0u;
                         for (uint32_t u0 = 0; u0 < nbm; u0 += kBmLoads) {
                             uint32_t w[kBmLoads];
 #pragma unroll
+                            for (uint32_t i = 0; i < kBmLoads; ++i) w[i] = wn[i];
+#pragma unroll
                             for (uint32_t i = 0; i < kBmLoads; ++i)
-                                w[i] = u0 + i < nbm ? __ldg(rows + (size_t)bm_row[u0 + i] * (size_t)ix.bm_words + j) : 0u;
+                                wn[i] = u0 + kBmLoads + i < nbm
+                                            ? __ldg(rows + (size_t)bm_row[u0 + kBmLoads + i] * (size_t)ix.bm_words + j)
+                                            : 0u;
                             if (SMALL) {
                                 // the eight rows' bits into the planes by a carry-save adder
                                 // tree (full adders: sum a^b^c, carry majority(a,b,c)); a group
