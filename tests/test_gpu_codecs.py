@@ -111,3 +111,7 @@ def test_bp32_block_segments_dense_exact(genie, oracle, codec):
     ids, cnt, sc = bt.run(qb, scores=True)
     oid, ocnt, osc, _ = oracle.Index(values).search(qb.as_oracle_batch())
     assert np.array_equal(cnt, ocnt) and np.array_equal(ids, oid) and np.array_equal(sc, osc)
+    # parts of several tiles: a segment straddling a tile bound is cut in both
+    bt.set_tuning(dense_tile=16384, dense_part_work=4 * 16384)
+    ids, cnt, sc = bt.run(qb, scores=True)
+    assert np.array_equal(cnt, ocnt) and np.array_equal(ids, oid) and np.array_equal(sc, osc)

@@ -17,6 +17,8 @@ def _qb(genie, b):
     dict(dense_bitmaps=-1),                         # directories, every list from its ids
     dict(dense_tile=40016, dense_bitmaps=2),        # another tile size, bitmaps for weighted queries only
     dict(dense_tile=65536, dense_bitmaps=1),        # other directory sizes, bitmaps for bytes only
+    dict(dense_tile=40016, dense_part_work=3 * 40016),  # parts of several tiles (running top-k across tiles)
+    dict(dense_tile=65536, dense_part_work=1, dense_bitmaps=3),  # below one tile: one tile per part
 ])
 def test_dense_paths_equal_oracle(genie, oracle, tiles):
     from genie_gb300 import workloads
