@@ -1414,7 +1414,7 @@ Tuning default_tuning() {
     t.dense_tile_u32 = 36864;        // 144 KiB of 4-byte counters
     t.dense_threads = 1024;
     t.sparse_max_total = 16 * 16896;
-    t.dense_part_work = 2 * 172032;  // two 172,032-object 1-byte tiles per dense part
+    t.dense_part_work = 147456;      // one 1-byte tile (four 4-byte tiles) per dense part
     t.sparse_ctas_per_sm = 2;
     t.dense_ctas_per_sm = 1;
     t.sparse_load_pct = 50;
