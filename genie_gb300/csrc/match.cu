@@ -1100,7 +1100,6 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
         const uint64_t ntiles = (N + tile_cap - 1) / tile_cap;
         const uint64_t t0 = ntiles * p / P, t1 = ntiles * (p + 1) / P;
         const bool single = qi.n_units <= kItemChunk;
-        const bool weighted = (qi.flags & kFlagWeighted) != 0;
         if (tid == 0) {
             s_nS = 0;
             s_nbm = 0;
@@ -1378,7 +1377,6 @@ __device__ __forceinline__ void dense_list(const DevIndex &ix, const DevQueries 
         const uint32_t nS = s_nS;
         for (uint32_t i = tid; i < nS; i += blockDim.x) cand[i] = S[i];
         __syncthreads();
-        (void)weighted;
         finish_part(ix, W, T, Q, q, p, qi, cand, nS, ss, false);
         __syncthreads();
     }
