@@ -379,6 +379,28 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
     };
     float best_ms = 1e30f;
     Tuning best = base;
+    // three timed launches of the current tuning after one untimed; a tuning
+    // whose launch fails is skipped, a device error ends the search
+    auto try_current = [&]() -> int {
+        float total = 0.0f;
+        bool ok = true;
+        for (int it = 0; it < 4 && ok; ++it) {
+            if (genie_batch_launch(b, nullptr)) {
+                ok = false;
+                break;
+            }
+            float ms = 0.0f;
+            genie_batch_last_stats(b, nullptr, &ms);
+            if (it > 0) total += ms;
+        }
+        cudaError_t e = cudaStreamSynchronize(b->stream);
+        if (e) return cuda_fail(e, "autotune");
+        if (ok && total < best_ms) {
+            best_ms = total;
+            best = b->tuning;
+        }
+        return GENIE_OK;
+    };
     for (const Cand &c : cands) {
         genie_tuning t{};
         t.sparse_slots = c.slots;
@@ -389,20 +411,7 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
         t.bitmap_bits = c.bits;
         t.dense_bitmaps = c.dbm;
         if (genie_batch_set_tuning(b, &t)) continue;
-        float total = 0.0f;
-        bool ok = true;
-        for (int it = 0; it < 4 && ok; ++it) {
-            if (genie_batch_launch(b, nullptr)) { ok = false; break; }
-            float ms = 0.0f;
-            genie_batch_last_stats(b, nullptr, &ms);
-            if (it > 0) total += ms;
-        }
-        cudaError_t e = cudaStreamSynchronize(b->stream);
-        if (e) return cuda_fail(e, "autotune");
-        if (ok && total < best_ms) {
-            best_ms = total;
-            best = b->tuning;
-        }
+        if ((rc = try_current())) return rc;
         b->tuning = base;
     }
     // then the objects per dense part, in whole tiles of the chosen tile size
@@ -411,20 +420,7 @@ int genie_batch_autotune(genie_batch *b, const genie_queries *sample, genie_tuni
         b->tuning = first;
         b->tuning.dense_part_work = tiles * first.dense_tile_u8;
         b->graph_valid = false;
-        float total = 0.0f;
-        bool ok = true;
-        for (int it = 0; it < 4 && ok; ++it) {
-            if (genie_batch_launch(b, nullptr)) { ok = false; break; }
-            float ms = 0.0f;
-            genie_batch_last_stats(b, nullptr, &ms);
-            if (it > 0) total += ms;
-        }
-        cudaError_t e = cudaStreamSynchronize(b->stream);
-        if (e) return cuda_fail(e, "autotune");
-        if (ok && total < best_ms) {
-            best_ms = total;
-            best = b->tuning;
-        }
+        if ((rc = try_current())) return rc;
     }
     b->tuning = best;
     b->graph_valid = false;
